@@ -1,0 +1,365 @@
+"""axbc_gb300: GB300-native sampled-Brandes betweenness centrality.
+
+Python binding of the C ABI in ``include/axbc.h`` (``libaxbc_gb300.so``, built
+in-tree by ``axbc_gb300.build``).  Every call goes to the CUDA library; there is
+no CPU fallback: if the library is missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libaxbc_gb300.so")
+MAX_BATCH = 32
+_LIB = None
+
+
+class AxbcError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"axbc status {status}: {msg}")
+        self.status = status
+
+
+class PivotStats(C.Structure):
+    _fields_ = [("nvisited", C.c_uint64), ("all", C.c_uint64), ("te", C.c_uint64),
+                ("levels", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self):
+        return dict(nvisited=self.nvisited, all=self.all, te=self.te, levels=self.levels)
+
+
+class RunParams(C.Structure):
+    _fields_ = [("z", C.c_int32), ("bader_c", C.c_int32), ("nbfs", C.c_uint64),
+                ("nchecks", C.c_uint32), ("H", C.c_int32), ("seed", C.c_int64),
+                ("batch_width", C.c_int32), ("pad", C.c_int32)]
+
+
+class RunResult(C.Structure):
+    _fields_ = [("nrounds", C.c_uint64), ("skipped", C.c_uint64), ("dropped", C.c_uint64),
+                ("rounds", C.c_uint64), ("te", C.c_uint64), ("stopped", C.c_int32),
+                ("batches", C.c_int32)]
+
+
+# name -> (restype, argtypes) of every entry point this binding uses
+_P = C.c_void_p
+_U32P = C.POINTER(C.c_uint32)
+_SIGS = {
+    "axbc_status_str": (C.c_char_p, [C.c_int]),
+    "axbc_last_error": (C.c_char_p, []),
+    "axbc_version": (C.c_char_p, []),
+    "axbc_edges_to_csc": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_int, C.c_int,
+                                    C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_uint64),
+                                    C.POINTER(_P), C.POINTER(C.c_uint64)]),
+    "axbc_host_free": (None, [_P]),
+    "axbc_read_edge_file": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(_P),
+                                      C.POINTER(C.c_uint64)]),
+    "axbc_graph_create": (C.c_int, [_P, _P, C.c_uint64, C.c_uint64, _P, C.POINTER(_P)]),
+    "axbc_graph_generate_rmat": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_int,
+                                           C.POINTER(_P)]),
+    "axbc_graph_generate_grid": (C.c_int, [C.c_uint32, C.c_double, C.c_double, C.c_uint64,
+                                           C.POINTER(_P)]),
+    "axbc_graph_destroy": (C.c_int, [_P]),
+    "axbc_graph_info": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                  C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
+    "axbc_graph_get_deg": (C.c_int, [_P, _P]),
+    "axbc_graph_get_csc": (C.c_int, [_P, _P, _P, _P]),
+    "axbc_graph_degree2": (C.c_int, [_P, _P]),
+    "axbc_graph_sum_deg_neigh": (C.c_int, [_P, _P]),
+    "axbc_graph_lcc": (C.c_int, [_P, _P]),
+    "axbc_ctx_create": (C.c_int, [_P, _P, C.POINTER(_P)]),
+    "axbc_ctx_destroy": (C.c_int, [_P]),
+    "axbc_ctx_reset": (C.c_int, [_P]),
+    "axbc_ctx_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "axbc_ctx_set_tuning": (C.c_int, [_P, C.c_double, C.c_double]),
+    "axbc_run_pivot": (C.c_int, [_P, C.c_uint32, C.c_double, C.c_int, C.POINTER(PivotStats)]),
+    "axbc_run_batch": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, _P]),
+    "axbc_run_sampled": (C.c_int, [_P, C.POINTER(RunParams), C.POINTER(RunResult)]),
+    "axbc_get_pivots": (C.c_int, [_P, _P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "axbc_get_checks": (C.c_int, [_P, _P, C.c_uint32]),
+    "axbc_get_bc": (C.c_int, [_P, _P]),
+    "axbc_get_delta": (C.c_int, [_P, _P]),
+    "axbc_get_sigma": (C.c_int, [_P, _P]),
+    "axbc_get_levels": (C.c_int, [_P, _P]),
+    "axbc_get_batch_source": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+    "axbc_bc_device_ptr": (C.c_int, [_P, C.POINTER(_P)]),
+    "axbc_ctx_sync": (C.c_int, [_P]),
+    "axbc_ctx_profile": (C.c_int, [_P, C.c_int]),
+    "axbc_ctx_profile_read": (C.c_int, [_P, _P, _P, _P, C.c_int]),
+    "axbc_ctx_launches": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+}
+
+PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bwd",
+              "batch_bwd_combine", "batch_update", "sampler", "plain_fwd", "plain_bwd",
+              "plain_other"]
+# kernel names behind each profiling kind (for matching ncu launch lists)
+PROF_KERNELS = {"batch_fwd_push": "k_fwd_push_m", "batch_fwd_pull": "k_fwd_pull_m",
+                "batch_level_stats": "k_level_stats", "batch_bwd": "k_bwd_m",
+                "batch_bwd_combine": "k_bwd_combine_m", "batch_update": "k_update_m",
+                "sampler": "k_sampler", "plain_fwd": "k_fwd_push1", "plain_bwd": "k_bwd1",
+                "plain_other": "k_update1"}
+
+
+def lib():
+    """Load libaxbc_gb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise AxbcError(-1, f"{LIB_PATH} is missing: run `python -m axbc_gb300.build` "
+                                "(the CUDA library is required; there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _check(rc):
+    if rc != 0:
+        raise AxbcError(rc, lib().axbc_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def version() -> str:
+    return lib().axbc_version().decode()
+
+
+def edges_to_csc(edges, n, undirected=True, H=0):
+    """Reference graph pipeline on the host: returns (col, row, reach, removed)."""
+    e = np.ascontiguousarray(np.asarray(edges, dtype=np.uint64).reshape(-1, 2))
+    col, row, reach = _P(), _P(), _P()
+    m, rem = C.c_uint64(), C.c_uint64()
+    L = lib()
+    _check(L.axbc_edges_to_csc(_ptr(e), len(e), n, int(undirected), H, C.byref(col),
+                               C.byref(row), C.byref(m), C.byref(reach), C.byref(rem)))
+    try:
+        colv = np.ctypeslib.as_array(C.cast(col, _U32P), (n + 1,)).copy()
+        rowv = (np.ctypeslib.as_array(C.cast(row, _U32P), (m.value,)).copy()
+                if m.value else np.zeros(0, np.uint32))
+        reachv = np.ctypeslib.as_array(C.cast(reach, _U32P), (n,)).copy()
+    finally:
+        for p in (col, row, reach):
+            L.axbc_host_free(p)
+    return colv, rowv, reachv, rem.value
+
+
+def read_edge_file(path, n):
+    out, ne = _P(), C.c_uint64()
+    L = lib()
+    _check(L.axbc_read_edge_file(path.encode(), n, C.byref(out), C.byref(ne)))
+    try:
+        if ne.value == 0:
+            return np.zeros((0, 2), np.uint64)
+        arr = np.ctypeslib.as_array(C.cast(out, C.POINTER(C.c_uint64)), (2 * ne.value,)).copy()
+    finally:
+        L.axbc_host_free(out)
+    return arr.reshape(-1, 2)
+
+
+class Graph:
+    """A graph resident on the current CUDA device (reference CSC layout)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        n, m, b, sym = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_int()
+        _check(lib().axbc_graph_info(handle, C.byref(n), C.byref(m), C.byref(b), C.byref(sym)))
+        self.n, self.m, self.bytes, self.symmetric = n.value, m.value, b.value, bool(sym.value)
+
+    @classmethod
+    def from_csc(cls, col, row, reach=None):
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        row = np.ascontiguousarray(row, dtype=np.uint32)
+        rch = None if reach is None else np.ascontiguousarray(reach, dtype=np.uint32)
+        h = _P()
+        _check(lib().axbc_graph_create(_ptr(col), _ptr(row), len(col) - 1, len(row), _ptr(rch),
+                                       C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, scale, edgefactor=16, seed=23, directed=False, H=0):
+        h = _P()
+        _check(lib().axbc_graph_generate_rmat(scale, edgefactor, seed, int(directed), H,
+                                              C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def grid(cls, side, drop_prob=0.02, longrange_frac=1e-4, seed=7):
+        h = _P()
+        _check(lib().axbc_graph_generate_grid(side, drop_prob, longrange_frac, seed, C.byref(h)))
+        return cls(h)
+
+    def csc(self):
+        col = np.empty(self.n + 1, np.uint32)
+        row = np.empty(max(self.m, 1), np.uint32)
+        reach = np.empty(self.n, np.uint32)
+        _check(lib().axbc_graph_get_csc(self._h, _ptr(col), _ptr(row), _ptr(reach)))
+        return col, row[:self.m], reach
+
+    def deg(self):
+        out = np.empty(self.n, np.uint32)
+        _check(lib().axbc_graph_get_deg(self._h, _ptr(out)))
+        return out
+
+    def degree2(self):
+        out = np.empty(self.n, np.uint32)
+        _check(lib().axbc_graph_degree2(self._h, _ptr(out)))
+        return out
+
+    def sum_deg_neigh(self):
+        out = np.empty(self.n, np.uint32)
+        _check(lib().axbc_graph_sum_deg_neigh(self._h, _ptr(out)))
+        return out
+
+    def lcc(self):
+        out = np.empty(self.n, np.float32)
+        _check(lib().axbc_graph_lcc(self._h, _ptr(out)))
+        return out
+
+    def close(self):
+        if self._h:
+            lib().axbc_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """BC state for one graph: bc, per-pivot state, batch state, sampler."""
+
+    def __init__(self, graph: Graph, stream=None):
+        self.graph = graph
+        h = _P()
+        _check(lib().axbc_ctx_create(graph._h, stream, C.byref(h)))
+        self._h = h
+        self.n = graph.n
+
+    @property
+    def bytes(self):
+        b = C.c_uint64()
+        _check(lib().axbc_ctx_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def set_tuning(self, push_factor_single=1.0, push_factor_batch=1.0):
+        _check(lib().axbc_ctx_set_tuning(self._h, push_factor_single, push_factor_batch))
+
+    def reset(self):
+        _check(lib().axbc_ctx_reset(self._h))
+
+    def run_pivot(self, v0, p, H=0):
+        st = PivotStats()
+        _check(lib().axbc_run_pivot(self._h, int(v0), float(p), H, C.byref(st)))
+        return st.as_dict()
+
+    def run_batch(self, v0s, ps, H=0, stats=True):
+        v = np.ascontiguousarray(v0s, dtype=np.uint32)
+        p = np.ascontiguousarray(ps, dtype=np.float64)
+        k = len(v)
+        st = (PivotStats * k)() if stats else None
+        _check(lib().axbc_run_batch(self._h, _ptr(v), _ptr(p), k, H,
+                                    C.cast(st, _P) if stats else None))
+        return [s.as_dict() for s in st] if stats else None
+
+    def run_sampled(self, z=0, nbfs=1, bader_c=1, nchecks=1, H=0, seed=4343543, W=1):
+        prm = RunParams(z, bader_c, nbfs, nchecks, H, seed, W, 0)
+        res = RunResult()
+        _check(lib().axbc_run_sampled(self._h, C.byref(prm), C.byref(res)))
+        cnt = C.c_uint64()
+        _check(lib().axbc_get_pivots(self._h, None, None, 0, C.byref(cnt)))
+        piv = np.zeros(cnt.value, np.uint32)
+        pr = np.zeros(cnt.value, np.float64)
+        _check(lib().axbc_get_pivots(self._h, _ptr(piv), _ptr(pr), cnt.value, C.byref(cnt)))
+        chk = np.zeros(max(nchecks, 1), np.uint32)
+        _check(lib().axbc_get_checks(self._h, _ptr(chk), nchecks))
+        return dict(nrounds=res.nrounds, skipped=res.skipped, dropped=res.dropped,
+                    ui_end=res.rounds, te=res.te, stopped=bool(res.stopped),
+                    batches=res.batches, pivots=piv, probs=pr, checks=chk[:nchecks])
+
+    def bc(self):
+        out = np.empty(self.n, np.float32)
+        _check(lib().axbc_get_bc(self._h, _ptr(out)))
+        return out
+
+    def delta(self):
+        out = np.empty(self.n, np.float32)
+        _check(lib().axbc_get_delta(self._h, _ptr(out)))
+        return out
+
+    def sigma(self):
+        out = np.empty(self.n, np.uint32)
+        _check(lib().axbc_get_sigma(self._h, _ptr(out)))
+        return out
+
+    def levels(self):
+        out = np.empty(self.n, np.int32)
+        _check(lib().axbc_get_levels(self._h, _ptr(out)))
+        return out
+
+    def batch_source(self, s):
+        sig = np.empty(self.n, np.uint32)
+        lvl = np.empty(self.n, np.int32)
+        dl = np.empty(self.n, np.float32)
+        _check(lib().axbc_get_batch_source(self._h, s, _ptr(sig), _ptr(lvl), _ptr(dl)))
+        return sig, lvl, dl
+
+    def bc_device_ptr(self) -> int:
+        p = _P()
+        _check(lib().axbc_bc_device_ptr(self._h, C.byref(p)))
+        return p.value
+
+    def sync(self):
+        _check(lib().axbc_ctx_sync(self._h))
+
+    def profile(self, enable=True):
+        """Record CUDA events around every kernel launch of this context."""
+        _check(lib().axbc_ctx_profile(self._h, int(enable)))
+
+    def profile_read(self):
+        """{kind: (ms, launches, algorithmic bytes)} since profile() / the last read."""
+        k = len(PROF_KINDS)
+        ms = np.zeros(k, np.float64)
+        cnt = np.zeros(k, np.uint64)
+        by = np.zeros(k, np.float64)
+        _check(lib().axbc_ctx_profile_read(self._h, _ptr(ms), _ptr(cnt), _ptr(by), k))
+        return {PROF_KINDS[i]: (float(ms[i]), int(cnt[i]), float(by[i])) for i in range(k)}
+
+    @property
+    def launches(self):
+        v = C.c_uint64()
+        _check(lib().axbc_ctx_launches(self._h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().axbc_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def exported_symbols():
+    """Names declared in include/*.h (read from the headers next to the package)."""
+    import re
+    names = []
+    inc = os.path.join(os.path.dirname(_HERE), "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            txt = open(os.path.join(inc, f)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names += re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt)
+    skip = {"if", "for", "while", "return", "sizeof", "defined"}
+    return sorted({n for n in names if n not in skip and not n.isupper()})

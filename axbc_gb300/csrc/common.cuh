@@ -1,0 +1,272 @@
+// Internal declarations shared by the axbc_gb300 CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/axbc.h"
+
+// ---------------------------------------------------------------- constants
+// Canonical accumulation order of one vertex's dependency sum (identical in
+// the plain and the batched kernels): successor terms in adjacency order,
+// CHUNK positions summed as a balanced binary tree, chunk sums added left to
+// right inside SPAN positions, span sums added left to right onto reach[v].
+// Vertices with more than SPAN neighbours are "heavy": their spans are
+// separate work items whose partial sums are combined in span order.
+#define AXBC_CHUNK 32
+#define AXBC_SPAN 1024
+#define AXBC_SAMPLE_BLOCK 1024
+#define AXBC_W 32
+#define FULL_MASK 0xffffffffu
+
+// ---------------------------------------------------------------- errors
+void axbc_set_error(const char *fmt, ...);
+int axbc_cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define CU(call)                                                                  \
+    do {                                                                          \
+        cudaError_t _e = (call);                                                  \
+        if (_e != cudaSuccess) return axbc_cuda_fail(_e, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define CU_LAUNCH(what)                                                           \
+    do {                                                                          \
+        cudaError_t _e = cudaGetLastError();                                      \
+        if (_e != cudaSuccess) return axbc_cuda_fail(_e, what, __FILE__, __LINE__); \
+    } while (0)
+
+#define CHECK_ARG(cond, msg)                                                      \
+    do {                                                                          \
+        if (!(cond)) {                                                            \
+            axbc_set_error("%s", msg);                                            \
+            return AXBC_ERR_INVALID;                                              \
+        }                                                                         \
+    } while (0)
+
+#define TRY(call)                                                                 \
+    do {                                                                          \
+        int _rc = (call);                                                         \
+        if (_rc != AXBC_OK) return _rc;                                           \
+    } while (0)
+
+// ---------------------------------------------------------------- graph
+// One direction of adjacency on the device.  `fwd` is the reference's CSC
+// (column c lists the r of edges (r,c)); `rev` is its transpose, used when a
+// forward level pulls into unvisited vertices.  For a symmetric graph rev
+// aliases fwd.
+struct Adj {
+    uint64_t n = 0, m = 0;
+    uint32_t *col = nullptr;  // n+1
+    uint32_t *row = nullptr;  // m
+    // heavy vertices (degree > SPAN): one work item per span
+    uint32_t n_heavy = 0;
+    uint64_t n_heavy_items = 0;
+    uint32_t *heavy_v = nullptr;      // n_heavy vertex ids
+    uint32_t *heavy_first = nullptr;  // n_heavy first item index
+    uint32_t *hitem_v = nullptr;      // n_heavy_items
+    uint32_t *hitem_k = nullptr;      // span index of the item
+    bool owns = true;
+};
+
+struct axbc_graph {
+    int device = 0;
+    uint64_t n = 0, m = 0;
+    int symmetric = 1;
+    Adj fwd, rev;
+    uint32_t *reach = nullptr;  // n
+    uint64_t bytes = 0;
+    uint32_t max_deg = 0;
+    // static pivot distributions, built on first use
+    bool have_deg_dist = false;
+    uint32_t *deg2p = nullptr;    // uint32 prefix of (uint32)deg^2 (wraps)
+    uint32_t *sdn = nullptr;      // neighbour degree sums
+    uint32_t *seg_end = nullptr;  // ends of the non-decreasing runs of deg2p
+    uint32_t n_seg = 0;
+    uint32_t sum_deg = 0;
+    bool have_lcc = false;
+    float *lcc = nullptr;
+    double *lcc_local = nullptr;
+    double *lcc_csum = nullptr;
+    double S_lcc = 0;
+};
+
+// graph helpers (graph.cu)
+int axbc_graph_build_device(axbc_graph *g, const uint32_t *d_col, const uint32_t *d_row,
+                            const uint32_t *d_reach, cudaStream_t s);
+int axbc_build_deg_dist(axbc_graph *g, cudaStream_t s);
+int axbc_build_lcc(axbc_graph *g, cudaStream_t s);
+// hierarchical prefix of n float weights (sampler.cu)
+int axbc_hprefix_launch(const float *w, uint64_t n, double *local, double *csum, cudaStream_t s);
+
+// ---------------------------------------------------------------- context
+struct PivotCounters {  // device, single-source
+    uint32_t qtail;
+    uint32_t pad;
+    unsigned long long newdeg;  // degree sum of vertices discovered this level
+    unsigned long long reach_sum;
+    unsigned long long visited_rdeg;  // in-degree sum of visited vertices
+};
+
+struct BatchInfo {  // device, one multi-source batch
+    uint32_t nsrc;
+    uint32_t napply;      // sources whose update is applied (Bader replay)
+    uint32_t srcmask;
+    uint32_t depth0mask;  // sources whose BFS ended at level 2
+    uint32_t root[AXBC_W];
+    double p[AXBC_W];
+    // per-source totals accumulated by the level-stats kernel
+    unsigned long long nvis[AXBC_W];
+    unsigned long long rsum[AXBC_W];
+    unsigned long long te[AXBC_W];
+    // per-level scratch read back by the host
+    unsigned long long lvl_new[AXBC_W];
+    unsigned long long front_deg;
+    unsigned long long unvis_deg;
+    unsigned long long lvl_te;  // degree sum over the level's new (vertex, pivot) pairs
+    uint32_t any_new;
+    uint32_t task_ctr[4];
+    int32_t H;
+};
+
+struct SamplerState;  // sampler.cu
+
+// Kernel kinds timed by the profiling hooks (axbc_ctx_profile).
+enum {
+    KP_FWD_PUSH = 0,   // batched forward, push
+    KP_FWD_PULL,       // batched forward, pull
+    KP_LEVEL_STATS,    // batched level bookkeeping
+    KP_BWD,            // batched backward
+    KP_BWD_COMBINE,    // batched heavy-vertex combine
+    KP_UPDATE,         // batched bc update + delta extraction
+    KP_SAMPLER,        // sampler, Bader replay, prefix sums
+    KP_PLAIN_FWD,      // plain forward level
+    KP_PLAIN_BWD,      // plain backward level (+ combine)
+    KP_PLAIN_OTHER,    // plain reset / root / reach sum / update
+    KP_NKINDS
+};
+
+struct ProfRec {
+    int kind;
+    double bytes;  // algorithmic bytes of the launch
+    cudaEvent_t a, b;
+};
+
+struct axbc_ctx {
+    axbc_graph *g = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    float *bc = nullptr;
+    float *delta_last = nullptr;
+    bool delta_last_valid = false;
+    // plain single-source state
+    int32_t *lvl = nullptr;
+    uint32_t *sigma = nullptr;
+    float *delta = nullptr;
+    uint32_t *queue = nullptr;
+    float *partial = nullptr;  // heavy span partials (fwd heavy items)
+    PivotCounters *pc = nullptr;
+    PivotCounters *pc_host = nullptr;  // pinned
+    std::vector<uint64_t> levstart;
+    uint64_t s_front_deg = 0, s_prev_newdeg = 0, s_visited_rdeg = 0;  // direction choice
+    // multi-source batch state
+    uint32_t *seen = nullptr;
+    std::vector<uint32_t *> fmask;  // one n-word mask array per level
+    uint32_t *msigma = nullptr;     // n*32
+    float *mdelta = nullptr;        // n*32
+    float *mpartial = nullptr;      // heavy items * 32
+    BatchInfo *bi = nullptr;
+    BatchInfo *bi_host = nullptr;  // pinned
+    int last_batch_levels = 0;
+    int last_batch_nsrc = 0;
+    int last_Ls[AXBC_W] = {0};  // first empty level of each pivot of the last batch
+    // sampler
+    SamplerState *ss = nullptr;
+    SamplerState *ss_host = nullptr;  // pinned
+    uint8_t *used = nullptr;          // n: pivot already drawn
+    uint32_t *checks = nullptr;
+    float *checkval = nullptr;  // Bader replay scratch, one per check vertex
+    uint32_t nchecks_cap = 0;
+    double *dyn_local = nullptr;
+    double *dyn_csum = nullptr;
+    double *dyn_local2 = nullptr;
+    double *dyn_csum2 = nullptr;
+    float *wtmp = nullptr;
+    std::vector<uint32_t> run_pivots;
+    std::vector<double> run_probs;
+    std::vector<uint32_t> run_checks;
+    // profiling: launch count always, event pairs when prof_on
+    uint64_t launches = 0;
+    bool prof_on = false;
+    std::vector<ProfRec> prof;
+    std::vector<cudaEvent_t> ev_pool;
+    double level_te_prev = 0;  // degree sum of the previous level's new vertices
+    std::vector<double> level_te;
+    // tuning
+    double push_factor_single = 1.0;
+    double push_factor_batch = 1.0;
+    uint64_t bytes = 0;
+    int num_sms = 0;
+};
+
+// allocation with byte accounting
+int axbc_dalloc(void **p, size_t bytes, uint64_t *acct);
+void axbc_dfree(void *p);
+
+// single.cu / batch.cu
+int axbc_ensure_single(axbc_ctx *c);
+int axbc_single_reset(axbc_ctx *c);
+int axbc_single_set_root(axbc_ctx *c, uint32_t v0, int level, uint32_t sig);
+int axbc_single_forward_level(axbc_ctx *c, uint32_t qs, uint32_t nf, int level, uint64_t *nfrt);
+int axbc_single_backward_level(axbc_ctx *c, uint32_t ls, uint32_t nseg, int d);
+int axbc_single_reach_sum(axbc_ctx *c);
+int axbc_single_update(axbc_ctx *c, uint32_t v0, double p, const uint32_t *reach_v0_dev,
+                       uint64_t nvt_base, int add_all, int add_sum);
+int axbc_ensure_batch(axbc_ctx *c);
+int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H);
+int axbc_batch_apply(axbc_ctx *c);
+int axbc_batch_levels_alloc(axbc_ctx *c, int levels);
+
+// grid sizing
+int axbc_grid_for(const axbc_ctx *c, int threads_per_block, int blocks_per_sm);
+
+// profiling hooks around one kernel launch on c->stream
+void axbc_prof_start(axbc_ctx *c, int kind, double bytes);
+void axbc_prof_stop(axbc_ctx *c);
+struct ProfScope {
+    axbc_ctx *c;
+    ProfScope(axbc_ctx *cc, int kind, double bytes) : c(cc) { axbc_prof_start(c, kind, bytes); }
+    ~ProfScope() { axbc_prof_stop(c); }
+};
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// One successor's share of a dependency, in the reference's operation order
+// (scan_frt_mono: (delta[r] + 1) / sigma[r] * sigma[c]), rounded op by op.
+__device__ __forceinline__ float dep_term(float delta_r, uint32_t sigma_r, float sigma_c)
+{
+    return __fmul_rn(__fdiv_rn(__fadd_rn(delta_r, 1.0f), __uint2float_rn(sigma_r)), sigma_c);
+}
+
+// Balanced binary tree over the 32 lanes (pairs differing in bit 0 first).
+__device__ __forceinline__ float warp_tree_sum(float v)
+{
+#pragma unroll
+    for (int w = 1; w < 32; w <<= 1) v = __fadd_rn(v, __shfl_xor_sync(FULL_MASK, v, w));
+    return v;
+}
+
+// The bc increment of one pivot for a non-root vertex (update_bc,
+// src/cuda_kernels.cu:284): float(double(delta * (float)(reach_v0 + 1)) / p).
+__device__ __forceinline__ float bc_term(float delta_v, uint32_t reach_v0, double p)
+{
+    return __double2float_rn(__ddiv_rn((double)__fmul_rn(delta_v, __uint2float_rn(reach_v0 + 1u)), p));
+}
+// The root's increment (:277): reach_v0 * (nvisited - 2) converted to float.
+__device__ __forceinline__ float bc_root_term(uint32_t reach_v0, unsigned long long nvis_total)
+{
+    return __ull2float_rn((unsigned long long)reach_v0 * (nvis_total - 2ull));
+}

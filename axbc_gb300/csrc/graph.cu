@@ -1,0 +1,724 @@
+// Graphs on the device: upload of the reference's CSC, heavy-vertex work
+// items, transpose for directed inputs, device-side synthetic generators and
+// the static pivot distributions (degree^2 prefix, neighbour-degree sums,
+// local clustering coefficients).
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+int axbc_dalloc(void **p, size_t bytes, uint64_t *acct)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        axbc_set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        return AXBC_ERR_NOMEM;
+    }
+    if (acct) *acct += bytes;
+    return AXBC_OK;
+}
+
+void axbc_dfree(void *p)
+{
+    if (p) cudaFree(p);
+}
+
+// ------------------------------------------------------------------ upload
+
+static void heavy_lists(const uint32_t *col, uint64_t n, std::vector<uint32_t> &hv,
+                        std::vector<uint32_t> &hfirst, std::vector<uint32_t> &iv,
+                        std::vector<uint32_t> &ik, uint32_t *maxdeg)
+{
+    uint32_t md = 0;
+    for (uint64_t v = 0; v < n; v++) {
+        uint32_t d = col[v + 1] - col[v];
+        md = std::max(md, d);
+        if (d > AXBC_SPAN) {
+            hv.push_back((uint32_t)v);
+            hfirst.push_back((uint32_t)iv.size());
+            uint32_t spans = (d + AXBC_SPAN - 1) / AXBC_SPAN;
+            for (uint32_t k = 0; k < spans; k++) {
+                iv.push_back((uint32_t)v);
+                ik.push_back(k);
+            }
+        }
+    }
+    if (maxdeg) *maxdeg = std::max(*maxdeg, md);
+}
+
+static int upload_adj(Adj &a, const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
+                      uint64_t *acct, uint32_t *maxdeg)
+{
+    a.n = n;
+    a.m = m;
+    TRY(axbc_dalloc((void **)&a.col, (n + 1) * 4, acct));
+    TRY(axbc_dalloc((void **)&a.row, m * 4, acct));
+    CU(cudaMemcpy(a.col, col, (n + 1) * 4, cudaMemcpyHostToDevice));
+    if (m) CU(cudaMemcpy(a.row, row, m * 4, cudaMemcpyHostToDevice));
+    std::vector<uint32_t> hv, hf, iv, ik;
+    heavy_lists(col, n, hv, hf, iv, ik, maxdeg);
+    a.n_heavy = (uint32_t)hv.size();
+    a.n_heavy_items = iv.size();
+    TRY(axbc_dalloc((void **)&a.heavy_v, hv.size() * 4, acct));
+    TRY(axbc_dalloc((void **)&a.heavy_first, (hf.size() + 1) * 4, acct));
+    TRY(axbc_dalloc((void **)&a.hitem_v, iv.size() * 4, acct));
+    TRY(axbc_dalloc((void **)&a.hitem_k, ik.size() * 4, acct));
+    hf.push_back((uint32_t)iv.size());
+    if (!hv.empty()) CU(cudaMemcpy(a.heavy_v, hv.data(), hv.size() * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(a.heavy_first, hf.data(), hf.size() * 4, cudaMemcpyHostToDevice));
+    if (!iv.empty()) {
+        CU(cudaMemcpy(a.hitem_v, iv.data(), iv.size() * 4, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(a.hitem_k, ik.data(), ik.size() * 4, cudaMemcpyHostToDevice));
+    }
+    a.owns = true;
+    return AXBC_OK;
+}
+
+static void free_adj(Adj &a)
+{
+    if (!a.owns) {
+        a = Adj();
+        return;
+    }
+    axbc_dfree(a.col);
+    axbc_dfree(a.row);
+    axbc_dfree(a.heavy_v);
+    axbc_dfree(a.heavy_first);
+    axbc_dfree(a.hitem_v);
+    axbc_dfree(a.hitem_k);
+    a = Adj();
+}
+
+// transpose of a CSC: column r of the result lists, ascending, the columns c
+// whose list contains r
+static void transpose_host(const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
+                           std::vector<uint32_t> &tcol, std::vector<uint32_t> &trow)
+{
+    tcol.assign(n + 1, 0);
+    trow.resize(m);
+    for (uint64_t e = 0; e < m; e++) tcol[row[e] + 1]++;
+    for (uint64_t v = 0; v < n; v++) tcol[v + 1] += tcol[v];
+    std::vector<uint32_t> pos(tcol.begin(), tcol.end() - 1);
+    for (uint64_t c = 0; c < n; c++)
+        for (uint32_t e = col[c]; e < col[c + 1]; e++) trow[pos[row[e]]++] = (uint32_t)c;
+}
+
+static int graph_from_host(const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
+                           const uint32_t *reach, int known_symmetric, axbc_graph **out)
+{
+    axbc_graph *g = new axbc_graph();
+    CU(cudaGetDevice(&g->device));
+    g->n = n;
+    g->m = m;
+    int rc = upload_adj(g->fwd, col, row, n, m, &g->bytes, &g->max_deg);
+    if (rc) {
+        axbc_graph_destroy(g);
+        return rc;
+    }
+    bool sym = known_symmetric != 0;
+    std::vector<uint32_t> tcol, trow;
+    if (!sym) {
+        transpose_host(col, row, n, m, tcol, trow);
+        sym = std::equal(tcol.begin(), tcol.end(), col) &&
+              (m == 0 || std::equal(trow.begin(), trow.end(), row));
+    }
+    g->symmetric = sym;
+    if (sym) {
+        g->rev = g->fwd;
+        g->rev.owns = false;
+    } else {
+        rc = upload_adj(g->rev, tcol.data(), trow.data(), n, m, &g->bytes, &g->max_deg);
+        if (rc) {
+            axbc_graph_destroy(g);
+            return rc;
+        }
+    }
+    rc = axbc_dalloc((void **)&g->reach, n * 4, &g->bytes);
+    if (rc) {
+        axbc_graph_destroy(g);
+        return rc;
+    }
+    if (reach) CU(cudaMemcpy(g->reach, reach, n * 4, cudaMemcpyHostToDevice));
+    else CU(cudaMemset(g->reach, 0, n * 4));
+    *out = g;
+    return AXBC_OK;
+}
+
+extern "C" int axbc_graph_create(const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
+                                 const uint32_t *reach, axbc_graph **g)
+{
+    CHECK_ARG(g && col && (row || m == 0), "axbc_graph_create: null argument");
+    CHECK_ARG(n > 0 && n < 0xffffffffull, "axbc_graph_create: n must be in [1, 2^32-1)");
+    CHECK_ARG(col[0] == 0 && col[n] == m, "axbc_graph_create: col[0] must be 0 and col[n] == m");
+    for (uint64_t v = 0; v < n; v++)
+        CHECK_ARG(col[v] <= col[v + 1], "axbc_graph_create: col is not non-decreasing");
+    for (uint64_t e = 0; e < m; e++)
+        CHECK_ARG(row[e] < n, "axbc_graph_create: row id out of range");
+    return graph_from_host(col, row, n, m, reach, 0, g);
+}
+
+extern "C" int axbc_graph_destroy(axbc_graph *g)
+{
+    if (!g) return AXBC_OK;
+    free_adj(g->rev);
+    free_adj(g->fwd);
+    axbc_dfree(g->reach);
+    axbc_dfree(g->deg2p);
+    axbc_dfree(g->sdn);
+    axbc_dfree(g->seg_end);
+    axbc_dfree(g->lcc);
+    axbc_dfree(g->lcc_local);
+    axbc_dfree(g->lcc_csum);
+    delete g;
+    return AXBC_OK;
+}
+
+extern "C" int axbc_graph_info(const axbc_graph *g, uint64_t *n, uint64_t *m, uint64_t *bytes,
+                               int *symmetric)
+{
+    CHECK_ARG(g, "axbc_graph_info: null graph");
+    if (n) *n = g->n;
+    if (m) *m = g->m;
+    if (bytes) *bytes = g->bytes;
+    if (symmetric) *symmetric = g->symmetric;
+    return AXBC_OK;
+}
+
+__global__ void k_degrees(const uint32_t *__restrict__ col, uint32_t *__restrict__ deg, uint64_t n)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x)
+        deg[v] = col[v + 1] - col[v];
+}
+
+extern "C" int axbc_graph_get_deg(const axbc_graph *g, uint32_t *deg_host)
+{
+    CHECK_ARG(g && deg_host, "axbc_graph_get_deg: null argument");
+    uint32_t *d = nullptr;
+    TRY(axbc_dalloc((void **)&d, g->n * 4, nullptr));
+    k_degrees<<<1024, 256>>>(g->fwd.col, d, g->n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(deg_host, d, g->n * 4, cudaMemcpyDeviceToHost);
+    axbc_dfree(d);
+    if (e != cudaSuccess) return axbc_cuda_fail(e, "get_deg", __FILE__, __LINE__);
+    return AXBC_OK;
+}
+
+extern "C" int axbc_graph_get_csc(const axbc_graph *g, uint32_t *col_host, uint32_t *row_host,
+                                  uint32_t *reach_host)
+{
+    CHECK_ARG(g, "axbc_graph_get_csc: null graph");
+    if (col_host) CU(cudaMemcpy(col_host, g->fwd.col, (g->n + 1) * 4, cudaMemcpyDeviceToHost));
+    if (row_host && g->m) CU(cudaMemcpy(row_host, g->fwd.row, g->m * 4, cudaMemcpyDeviceToHost));
+    if (reach_host) CU(cudaMemcpy(reach_host, g->reach, g->n * 4, cudaMemcpyDeviceToHost));
+    return AXBC_OK;
+}
+
+// ------------------------------------------------------------ generators
+
+// splitmix64 finaliser: the counter-based random source of the generators
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// bijective scramble of [0, 2^bits): odd multiplies and xor-shifts mod 2^bits
+__device__ __forceinline__ uint32_t scramble(uint32_t x, int bits, uint64_t seed)
+{
+    const uint64_t mask = (bits >= 64) ? ~0ull : ((1ull << bits) - 1);
+    uint64_t y = x;
+    uint64_t a = (mix64(seed) | 1ull), b = mix64(seed + 1), c = (mix64(seed + 2) | 1ull);
+    y = (y * a + b) & mask;
+    y ^= y >> (bits / 2 + 1);
+    y = (y * c) & mask;
+    y ^= y >> (bits / 3 + 1);
+    y = (y * a + c) & mask;
+    return (uint32_t)y;
+}
+
+// key of a directed adjacency entry in CSC order: column (second vertex) in
+// the high half, row (first vertex) in the low half
+__host__ __device__ __forceinline__ uint64_t ckey(uint32_t u, uint32_t v) { return ((uint64_t)v << 32) | u; }
+
+// R-MAT: edge e descends `scale` levels choosing quadrant a/b/c/d with
+// probabilities .57/.19/.19/.05
+__global__ void k_rmat(uint64_t nedges, int scale, uint64_t seed, int directed,
+                       uint64_t *__restrict__ keys, unsigned long long *__restrict__ nkeys)
+{
+    const uint32_t TA = (uint32_t)(0.57 * 4294967296.0);
+    const uint32_t TB = (uint32_t)(0.76 * 4294967296.0);
+    const uint32_t TC = (uint32_t)(0.95 * 4294967296.0);
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nedges;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t u = 0, v = 0;
+        uint64_t h = 0;
+        for (int l = 0; l < scale; l++) {
+            if ((l & 1) == 0) h = mix64(seed ^ (e * 0xD6E8FEB86659FD93ull + (uint64_t)l));
+            uint32_t r = (l & 1) ? (uint32_t)(h >> 32) : (uint32_t)h;
+            uint32_t bu = 0, bv = 0;
+            if (r < TA) {
+            } else if (r < TB) {
+                bv = 1;
+            } else if (r < TC) {
+                bu = 1;
+            } else {
+                bu = 1;
+                bv = 1;
+            }
+            u = (u << 1) | bu;
+            v = (v << 1) | bv;
+        }
+        u = scramble(u, scale, seed * 31 + 7);
+        v = scramble(v, scale, seed * 31 + 7);
+        keys[2 * e] = ckey(u, v);
+        keys[2 * e + 1] = (directed || u == v) ? ~0ull : ckey(v, u);
+    }
+    (void)nkeys;
+}
+
+// grid edges: index < nh horizontal (x,y)-(x+1,y), else vertical (x,y)-(x,y+1)
+__global__ void k_grid(uint32_t side, uint64_t nh, uint64_t ntot, uint32_t keep_thr, uint64_t seed,
+                       uint64_t *__restrict__ keys, unsigned long long *__restrict__ kept)
+{
+    unsigned long long local = 0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ntot;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t a, b;
+        if (e < nh) {
+            uint32_t y = (uint32_t)(e / (side - 1)), x = (uint32_t)(e % (side - 1));
+            a = y * side + x;
+            b = a + 1;
+        } else {
+            uint64_t f = e - nh;
+            uint32_t y = (uint32_t)(f / side), x = (uint32_t)(f % side);
+            a = y * side + x;
+            b = a + side;
+        }
+        bool keep = (uint32_t)mix64(seed ^ (e * 0x9E3779B97F4A7C15ull)) >= keep_thr;
+        keys[2 * e] = keep ? ckey(a, b) : ~0ull;
+        keys[2 * e + 1] = keep ? ckey(b, a) : ~0ull;
+        local += keep;
+    }
+    atomicAdd(kept, local);
+}
+
+__global__ void k_longrange(uint64_t count, uint64_t nverts, uint64_t seed, uint64_t *__restrict__ keys)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < count;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t h = mix64(seed ^ (0xA5A5A5A5ull + e * 0xD6E8FEB86659FD93ull));
+        uint32_t a = (uint32_t)((h & 0xffffffffull) % nverts);
+        uint32_t b = (uint32_t)((h >> 32) % nverts);
+        keys[2 * e] = ckey(a, b);
+        keys[2 * e + 1] = (a == b) ? ~0ull : ckey(b, a);
+    }
+}
+
+// keep the first copy of every key, drop self-loops except `quirk` (the
+// lexicographically first (u,v) edge, which norm_graph always keeps),
+// src/axbc2d.c:818-841
+__global__ void k_mark(const uint64_t *__restrict__ keys, uint64_t nk, uint64_t quirk,
+                       uint8_t *__restrict__ flag)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nk;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t k = keys[i];
+        bool f = (k != ~0ull) && (i == 0 || keys[i - 1] != k);
+        uint32_t u = (uint32_t)k, v = (uint32_t)(k >> 32);
+        if (f && u == v && k != quirk) f = false;
+        flag[i] = f;
+    }
+}
+
+__global__ void k_split(const uint64_t *__restrict__ keys, uint64_t m, uint32_t *__restrict__ row,
+                        uint32_t *__restrict__ cnt)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t k = keys[i];
+        row[i] = (uint32_t)k;
+        atomicAdd(&cnt[(uint32_t)(k >> 32)], 1u);
+    }
+}
+
+// lexicographically smallest (u,v) = (row, column) among valid keys
+__global__ void k_min_uv(const uint64_t *__restrict__ keys, uint64_t nk, unsigned long long *out)
+{
+    unsigned long long best = ~0ull;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nk;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t k = keys[i];
+        if (k == ~0ull) continue;
+        unsigned long long uv = ((unsigned long long)(uint32_t)k << 32) | (k >> 32);
+        best = best < uv ? best : uv;
+    }
+    atomicMin(out, best);
+}
+
+// Sort device keys, dedupe, build the CSC on the device and wrap it in a graph.
+// H == 1 runs the one-degree reduction on the host.
+int axbc_edges_to_csc_host_H1(const uint64_t *sorted_uv, uint64_t ned, uint64_t n,
+                              std::vector<uint32_t> &col, std::vector<uint32_t> &row,
+                              std::vector<uint32_t> &reach);
+
+static int keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetric, int H,
+                         axbc_graph **out)
+{
+    cudaStream_t s = 0;
+    uint64_t *d_sorted = nullptr;
+    void *d_tmp = nullptr;
+    size_t tmp_bytes = 0;
+    int rc = AXBC_OK;
+    TRY(axbc_dalloc((void **)&d_sorted, nk * 8, nullptr));
+    // all 64 bits: the all-ones padding keys must sort last
+    cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, d_keys, d_sorted, (int64_t)nk, 0, 64, s);
+    rc = axbc_dalloc(&d_tmp, tmp_bytes, nullptr);
+    if (rc) {
+        axbc_dfree(d_sorted);
+        return rc;
+    }
+    cub::DeviceRadixSort::SortKeys(d_tmp, tmp_bytes, d_keys, d_sorted, (int64_t)nk, 0, 64, s);
+    axbc_dfree(d_tmp);
+    CU_LAUNCH("radix sort");
+
+    unsigned long long *d_min = nullptr;
+    TRY(axbc_dalloc((void **)&d_min, 8, nullptr));
+    CU(cudaMemset(d_min, 0xff, 8));
+    k_min_uv<<<1024, 256>>>(d_sorted, nk, d_min);
+    unsigned long long minuv = ~0ull;
+    CU(cudaMemcpy(&minuv, d_min, 8, cudaMemcpyDeviceToHost));
+    axbc_dfree(d_min);
+    uint64_t quirk = ~0ull;
+    if (minuv != ~0ull && (uint32_t)(minuv >> 32) == (uint32_t)minuv) quirk = ckey((uint32_t)minuv, (uint32_t)minuv);
+
+    uint8_t *d_flag = nullptr;
+    TRY(axbc_dalloc((void **)&d_flag, nk, nullptr));
+    k_mark<<<2048, 256>>>(d_sorted, nk, quirk, d_flag);
+    CU_LAUNCH("k_mark");
+    unsigned long long *d_nsel = nullptr;
+    TRY(axbc_dalloc((void **)&d_nsel, 8, nullptr));
+    tmp_bytes = 0;
+    cub::DeviceSelect::Flagged(nullptr, tmp_bytes, d_sorted, d_flag, d_keys, d_nsel, (int64_t)nk, s);
+    TRY(axbc_dalloc(&d_tmp, tmp_bytes, nullptr));
+    cub::DeviceSelect::Flagged(d_tmp, tmp_bytes, d_sorted, d_flag, d_keys, d_nsel, (int64_t)nk, s);
+    CU_LAUNCH("select");
+    unsigned long long m = 0;
+    CU(cudaMemcpy(&m, d_nsel, 8, cudaMemcpyDeviceToHost));
+    axbc_dfree(d_tmp);
+    axbc_dfree(d_nsel);
+    axbc_dfree(d_flag);
+    axbc_dfree(d_sorted);
+    if (m >= 0xffffffffull) {
+        axbc_set_error("graph has %llu adjacency entries; 32-bit offsets hold < 2^32", m);
+        return AXBC_ERR_RANGE;
+    }
+
+    if (H == 1) {
+        // host one-degree reduction on the (u,v)-sorted edge list; for a
+        // symmetric edge set the (column,row)-sorted keys read as (u,v) pairs
+        // are that list
+        std::vector<uint64_t> h(m);
+        CU(cudaMemcpy(h.data(), d_keys, m * 8, cudaMemcpyDeviceToHost));
+        std::vector<uint64_t> uv(2 * m);
+        for (uint64_t i = 0; i < m; i++) {
+            uv[2 * i] = h[i] >> 32;
+            uv[2 * i + 1] = (uint32_t)h[i];
+        }
+        if (!symmetric) {
+            axbc_set_error("one-degree reduction of a generated graph needs a symmetric graph");
+            return AXBC_ERR_INVALID;
+        }
+        std::vector<uint32_t> col, row, reach;
+        TRY(axbc_edges_to_csc_host_H1(uv.data(), m, n, col, row, reach));
+        return graph_from_host(col.data(), row.data(), n, row.size(), reach.data(), 1, out);
+    }
+
+    uint32_t *d_row = nullptr, *d_cnt = nullptr;
+    TRY(axbc_dalloc((void **)&d_row, m * 4, nullptr));
+    TRY(axbc_dalloc((void **)&d_cnt, (n + 1) * 4, nullptr));
+    CU(cudaMemset(d_cnt, 0, (n + 1) * 4));
+    k_split<<<2048, 256>>>(d_keys, m, d_row, d_cnt);
+    CU_LAUNCH("k_split");
+    std::vector<uint32_t> col(n + 1), cnt(n + 1);
+    CU(cudaMemcpy(cnt.data(), d_cnt, (n + 1) * 4, cudaMemcpyDeviceToHost));
+    col[0] = 0;
+    for (uint64_t v = 0; v < n; v++) col[v + 1] = col[v] + cnt[v];
+    std::vector<uint32_t> row(m);
+    CU(cudaMemcpy(row.data(), d_row, m * 4, cudaMemcpyDeviceToHost));
+    axbc_dfree(d_row);
+    axbc_dfree(d_cnt);
+    return graph_from_host(col.data(), row.data(), n, m, nullptr, symmetric, out);
+}
+
+extern "C" int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed, int directed,
+                                        int H, axbc_graph **g)
+{
+    CHECK_ARG(g, "axbc_graph_generate_rmat: null output");
+    CHECK_ARG(scale >= 1 && scale <= 30, "axbc_graph_generate_rmat: scale must be in [1,30]");
+    CHECK_ARG(edgefactor >= 1 && edgefactor <= 1024, "axbc_graph_generate_rmat: bad edgefactor");
+    CHECK_ARG(H == 0 || H == 1, "axbc_graph_generate_rmat: H must be 0 or 1");
+    const uint64_t n = 1ull << scale;
+    const uint64_t ne = n * (uint64_t)edgefactor;
+    uint64_t *d_keys = nullptr;
+    TRY(axbc_dalloc((void **)&d_keys, 2 * ne * 8, nullptr));
+    k_rmat<<<4096, 256>>>(ne, scale, seed, directed, d_keys, nullptr);
+    CU_LAUNCH("k_rmat");
+    int rc = keys_to_graph(d_keys, 2 * ne, n, !directed, H, g);
+    axbc_dfree(d_keys);
+    return rc;
+}
+
+extern "C" int axbc_graph_generate_grid(uint32_t side, double drop_prob, double longrange_frac,
+                                        uint64_t seed, axbc_graph **g)
+{
+    CHECK_ARG(g, "axbc_graph_generate_grid: null output");
+    CHECK_ARG(side >= 2 && side <= 32768, "axbc_graph_generate_grid: side must be in [2,32768]");
+    CHECK_ARG(drop_prob >= 0 && drop_prob < 1, "axbc_graph_generate_grid: bad drop probability");
+    const uint64_t n = (uint64_t)side * side;
+    const uint64_t nh = (uint64_t)(side - 1) * side, nv = nh, ntot = nh + nv;
+    uint64_t *d_keys = nullptr;
+    unsigned long long *d_kept = nullptr;
+    TRY(axbc_dalloc((void **)&d_kept, 8, nullptr));
+    CU(cudaMemset(d_kept, 0, 8));
+    // room for the long-range edges: at most longrange_frac * ntot of them
+    uint64_t lr_cap = (uint64_t)(longrange_frac * (double)ntot) + 1;
+    TRY(axbc_dalloc((void **)&d_keys, (2 * ntot + 2 * lr_cap) * 8, nullptr));
+    uint32_t thr = (uint32_t)(drop_prob * 4294967296.0);
+    k_grid<<<2048, 256>>>(side, nh, ntot, thr, seed, d_keys, d_kept);
+    CU_LAUNCH("k_grid");
+    unsigned long long kept = 0;
+    CU(cudaMemcpy(&kept, d_kept, 8, cudaMemcpyDeviceToHost));
+    uint64_t lr = (uint64_t)(longrange_frac * (double)kept);
+    if (lr > lr_cap) lr = lr_cap;
+    if (lr) k_longrange<<<256, 256>>>(lr, n, seed, d_keys + 2 * ntot);
+    CU_LAUNCH("k_longrange");
+    int rc = keys_to_graph(d_keys, 2 * ntot + 2 * lr, n, 1, 0, g);
+    axbc_dfree(d_keys);
+    axbc_dfree(d_kept);
+    return rc;
+}
+
+// ------------------------------------------------- static distributions
+
+// (uint32)deg^2, the low 32 bits of the square (src/axbc2d.c:2681-2685)
+__global__ void k_deg2(const uint32_t *__restrict__ col, uint32_t *__restrict__ out, uint64_t n)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t d = col[v + 1] - col[v];
+        out[v] = (uint32_t)(d * d);
+    }
+}
+
+// neighbour-degree sums, uint32 (sum_deg_neigh_func, src/axbc2d.c:1758-1845)
+__global__ void k_sdn(const uint32_t *__restrict__ col, const uint32_t *__restrict__ row,
+                      uint32_t *__restrict__ out, uint64_t n)
+{
+    const unsigned lane = lane_id();
+    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t v = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; v < n; v += nw) {
+        uint32_t s = 0;
+        for (uint32_t e = col[v] + lane; e < col[v + 1]; e += 32) {
+            uint32_t w = row[e];
+            s += col[w + 1] - col[w];
+        }
+        s = __reduce_add_sync(FULL_MASK, s);
+        if (lane == 0) out[v] = s;
+    }
+}
+
+// ends of the non-decreasing runs of a wrapping uint32 prefix
+__global__ void k_wraps(const uint32_t *__restrict__ p, uint64_t n, uint32_t *__restrict__ ends,
+                        uint32_t *__restrict__ count, uint32_t cap)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (p[i + 1] < p[i]) {
+            uint32_t k = atomicAdd(count, 1u);
+            if (k < cap) ends[k] = (uint32_t)(i + 1);
+        }
+    }
+}
+
+int axbc_build_deg_dist(axbc_graph *g, cudaStream_t s)
+{
+    if (g->have_deg_dist) return AXBC_OK;
+    const uint64_t n = g->n;
+    uint32_t *d2 = nullptr;
+    TRY(axbc_dalloc((void **)&d2, n * 4, nullptr));
+    TRY(axbc_dalloc((void **)&g->deg2p, n * 4, &g->bytes));
+    TRY(axbc_dalloc((void **)&g->sdn, n * 4, &g->bytes));
+    k_deg2<<<1024, 256, 0, s>>>(g->fwd.col, d2, n);
+    k_sdn<<<2048, 256, 0, s>>>(g->fwd.col, g->fwd.row, g->sdn, n);
+    CU_LAUNCH("deg2/sdn");
+    void *tmp = nullptr;
+    size_t tb = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, tb, d2, g->deg2p, (int64_t)n, s);
+    TRY(axbc_dalloc(&tmp, tb, nullptr));
+    cub::DeviceScan::InclusiveSum(tmp, tb, d2, g->deg2p, (int64_t)n, s);
+    CU_LAUNCH("deg2 scan");
+    axbc_dfree(tmp);
+    axbc_dfree(d2);
+    // run ends: the prefix wraps at most (total / 2^32) + 1 times
+    const uint32_t cap = 1u << 20;
+    uint32_t *ends = nullptr, *cnt = nullptr;
+    TRY(axbc_dalloc((void **)&ends, cap * 4, nullptr));
+    TRY(axbc_dalloc((void **)&cnt, 4, nullptr));
+    CU(cudaMemsetAsync(cnt, 0, 4, s));
+    k_wraps<<<1024, 256, 0, s>>>(g->deg2p, n, ends, cnt, cap);
+    CU_LAUNCH("k_wraps");
+    uint32_t nw = 0;
+    CU(cudaMemcpyAsync(&nw, cnt, 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    if (nw > cap) {
+        axbc_set_error("degree^2 prefix wraps too often");
+        return AXBC_ERR_RANGE;
+    }
+    std::vector<uint32_t> h(nw);
+    if (nw) CU(cudaMemcpy(h.data(), ends, nw * 4, cudaMemcpyDeviceToHost));
+    std::sort(h.begin(), h.end());
+    h.push_back((uint32_t)n);
+    g->n_seg = (uint32_t)h.size();
+    TRY(axbc_dalloc((void **)&g->seg_end, h.size() * 4, &g->bytes));
+    CU(cudaMemcpy(g->seg_end, h.data(), h.size() * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(&g->sum_deg, g->deg2p + n - 1, 4, cudaMemcpyDeviceToHost));
+    axbc_dfree(ends);
+    axbc_dfree(cnt);
+    g->have_deg_dist = true;
+    return AXBC_OK;
+}
+
+// |adj(w) ∩ adj(i)| without i, by binary search of the shorter list's entries
+// in the longer one (adjacency lists are sorted and duplicate-free)
+__device__ __forceinline__ uint32_t isect_count(const uint32_t *a, uint32_t da, const uint32_t *b,
+                                                uint32_t db, uint32_t skip)
+{
+    if (da > db) {
+        const uint32_t *t = a;
+        a = b;
+        b = t;
+        uint32_t td = da;
+        da = db;
+        db = td;
+    }
+    uint32_t c = 0;
+    for (uint32_t k = 0; k < da; k++) {
+        uint32_t x = a[k];
+        if (x == skip) continue;
+        uint32_t lo = 0, hi = db;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (b[mid] < x) lo = mid + 1;
+            else hi = mid;
+        }
+        c += (lo < db && b[lo] == x);
+    }
+    return c;
+}
+
+// lcc_func (src/axbc2d.c:1847-1935): counter(i) = sum over neighbours w of
+// |adj(w) \ {i} ∩ adj(i)|, uint32.  Lanes take neighbours; vertices with more
+// than SPAN neighbours are split over their span items.
+__global__ void k_lcc_count(Adj a, uint32_t *__restrict__ counter)
+{
+    const unsigned lane = lane_id();
+    const uint64_t ntask = a.n + a.n_heavy_items;
+    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; t < ntask; t += nw) {
+        uint32_t i, b0, b1;
+        if (t < a.n) {
+            i = (uint32_t)t;
+            uint32_t d = a.col[i + 1] - a.col[i];
+            if (d < 2 || d > AXBC_SPAN) continue;
+            b0 = a.col[i];
+            b1 = a.col[i + 1];
+        } else {
+            i = a.hitem_v[t - a.n];
+            uint32_t k = a.hitem_k[t - a.n];
+            b0 = a.col[i] + k * AXBC_SPAN;
+            b1 = min(a.col[i + 1], b0 + AXBC_SPAN);
+        }
+        const uint32_t *ai = a.row + a.col[i];
+        const uint32_t di = a.col[i + 1] - a.col[i];
+        uint32_t c = 0;
+        for (uint32_t e = b0 + lane; e < b1; e += 32) {
+            uint32_t w = a.row[e];
+            c += isect_count(a.row + a.col[w], a.col[w + 1] - a.col[w], ai, di, i);
+        }
+        c = __reduce_add_sync(FULL_MASK, c);
+        if (lane == 0 && c) atomicAdd(&counter[i], c);
+    }
+}
+
+__global__ void k_lcc_final(const uint32_t *__restrict__ col, const uint32_t *__restrict__ counter,
+                            float *__restrict__ out, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t d = col[i + 1] - col[i];
+        out[i] = (d < 2) ? 0.0f
+                         : __fdiv_rn(__uint2float_rn(counter[i]), __uint2float_rn(d * (d - 1u)));
+    }
+}
+
+int axbc_build_lcc(axbc_graph *g, cudaStream_t s)
+{
+    if (g->have_lcc) return AXBC_OK;
+    const uint64_t n = g->n;
+    uint32_t *cnt = nullptr;
+    TRY(axbc_dalloc((void **)&cnt, n * 4, nullptr));
+    TRY(axbc_dalloc((void **)&g->lcc, n * 4, &g->bytes));
+    TRY(axbc_dalloc((void **)&g->lcc_local, n * 8, &g->bytes));
+    TRY(axbc_dalloc((void **)&g->lcc_csum, ((n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK) * 8,
+                    &g->bytes));
+    CU(cudaMemsetAsync(cnt, 0, n * 4, s));
+    k_lcc_count<<<4096, 256, 0, s>>>(g->fwd, cnt);
+    k_lcc_final<<<1024, 256, 0, s>>>(g->fwd.col, cnt, g->lcc, n);
+    CU_LAUNCH("lcc");
+    TRY(axbc_hprefix_launch(g->lcc, n, g->lcc_local, g->lcc_csum, s));
+    const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    CU(cudaMemcpyAsync(&g->S_lcc, g->lcc_csum + nb - 1, 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    axbc_dfree(cnt);
+    g->have_lcc = true;
+    return AXBC_OK;
+}
+
+extern "C" int axbc_graph_degree2(axbc_graph *g, uint32_t *out_host)
+{
+    CHECK_ARG(g && out_host, "axbc_graph_degree2: null argument");
+    uint32_t *d = nullptr;
+    TRY(axbc_dalloc((void **)&d, g->n * 4, nullptr));
+    k_deg2<<<1024, 256>>>(g->fwd.col, d, g->n);
+    CU_LAUNCH("k_deg2");
+    cudaError_t e = cudaMemcpy(out_host, d, g->n * 4, cudaMemcpyDeviceToHost);
+    axbc_dfree(d);
+    if (e != cudaSuccess) return axbc_cuda_fail(e, "degree2", __FILE__, __LINE__);
+    return AXBC_OK;
+}
+
+extern "C" int axbc_graph_sum_deg_neigh(axbc_graph *g, uint32_t *out_host)
+{
+    CHECK_ARG(g && out_host, "axbc_graph_sum_deg_neigh: null argument");
+    TRY(axbc_build_deg_dist(g, 0));
+    CU(cudaMemcpy(out_host, g->sdn, g->n * 4, cudaMemcpyDeviceToHost));
+    return AXBC_OK;
+}
+
+extern "C" int axbc_graph_lcc(axbc_graph *g, float *out_host)
+{
+    CHECK_ARG(g && out_host, "axbc_graph_lcc: null argument");
+    TRY(axbc_build_lcc(g, 0));
+    CU(cudaMemcpy(out_host, g->lcc, g->n * 4, cudaMemcpyDeviceToHost));
+    return AXBC_OK;
+}

@@ -1,0 +1,579 @@
+// Pivot sampling on the device: the seven heuristics of -z, the drand48
+// stream, the rejection of already-drawn pivots, the degree-0 skip, the
+// bad-sample limit and Bader's stop test -- the loop of src/axbc2d.c:
+// 2729-3156 on one rank -- plus the driver that alternates sampling with the
+// batched Brandes pass.
+//
+// Float-weighted distributions (LCC, bc, delta, 1/(1+bc)) are sampled from a
+// hierarchical double prefix (block-local running sums plus a running sum of
+// block totals) instead of the reference's float running sum; the integer
+// degree^2 distribution keeps the reference's uint32 wrap-around.
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+struct SamplerState {
+    uint64_t rng;
+    uint64_t ui, nbfs, N;
+    int32_t z;
+    uint32_t dist_mix;
+    uint32_t lim;
+    uint32_t bader_c;
+    uint32_t nchecks;
+    int32_t W;
+    int32_t done, stopped;
+    uint64_t nrounds, skipped, dropped, te;
+    uint64_t nrounds_snap;
+    // this batch
+    int32_t nb;
+    uint32_t napply;
+    uint64_t skipped_run;
+    uint32_t v0[AXBC_W];
+    double p[AXBC_W];
+    uint64_t skip_before[AXBC_W];
+};
+
+struct SamplerDists {
+    // static
+    const uint32_t *col, *row, *deg2p, *seg_end, *sdn;
+    uint32_t n_seg, sum_deg;
+    const float *lcc;
+    const double *lcc_local, *lcc_csum;
+    // dynamic (this batch's snapshot)
+    const float *bc, *delta_last;
+    const double *bc_local, *bc_csum;  // prefix of bc (z 3, 6) or 1/(1+bc) (z 5)
+    const double *d_local, *d_csum;    // prefix of the last delta (z 4, 6)
+};
+
+// ------------------------------------------------------------ drand48
+__device__ __forceinline__ int64_t d_lrand48(uint64_t &x)
+{
+    x = (0x5DEECE66DULL * x + 0xBULL) & 0xFFFFFFFFFFFFULL;
+    return (int64_t)(x >> 17);
+}
+// uniform_int(max, min) in uint32 arithmetic (src/axbc2d.c:2155-2164)
+__device__ __forceinline__ uint32_t d_uniform_int(uint64_t &x, uint32_t max, uint32_t min)
+{
+    const uint32_t mod = max - min + 1u;
+    const int64_t r = d_lrand48(x);
+    if (mod == 0) return (uint32_t)r + min;
+    return (uint32_t)(r % (int64_t)mod) + min;
+}
+// uniform01 (src/axbc2d.c:2172-2176): lrand48() / RAND_MAX
+__device__ __forceinline__ double d_uniform01(uint64_t &x)
+{
+    return __ddiv_rn((double)d_lrand48(x), 2147483647.0);
+}
+
+// ------------------------------------------------- hierarchical prefix
+__global__ void k_hprefix_local(const float *__restrict__ w, uint64_t n, double *__restrict__ local,
+                                double *__restrict__ bsum, int mode, const SamplerState *ss)
+{
+    if (ss && (ss->done || ss->nrounds_snap == 0)) return;
+    const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < nb;
+         b += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t e = min((b + 1) * AXBC_SAMPLE_BLOCK, n);
+        double t = 0.0;
+        for (uint64_t i = b * AXBC_SAMPLE_BLOCK; i < e; i++) {
+            float x = w[i];
+            // mode 1: the weight 1/(1+bc) of heuristic 5 (src/axbc2d.c:2025-2058)
+            if (mode == 1) x = __fdiv_rn(1.0f, __fadd_rn(1.0f, x));
+            t = __dadd_rn(t, (double)x);
+            local[i] = t;
+        }
+        bsum[b] = t;
+    }
+}
+
+__global__ void k_hprefix_csum(double *csum, uint64_t nb, const SamplerState *ss)
+{
+    if (ss && (ss->done || ss->nrounds_snap == 0)) return;
+    double c = 0.0;
+    for (uint64_t b = 0; b < nb; b++) {
+        c = __dadd_rn(c, csum[b]);
+        csum[b] = c;
+    }
+}
+
+int axbc_hprefix_launch(const float *w, uint64_t n, double *local, double *csum, cudaStream_t s)
+{
+    const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    k_hprefix_local<<<(unsigned)((nb + 127) / 128), 128, 0, s>>>(w, n, local, csum, 0, nullptr);
+    k_hprefix_csum<<<1, 1, 0, s>>>(csum, nb, nullptr);
+    CU_LAUNCH("hprefix");
+    return AXBC_OK;
+}
+
+// first index whose prefix reaches r; *found = 0 if the total is NaN or < r
+__device__ uint64_t d_hsearch(const double *local, const double *csum, uint64_t n, double r,
+                              int *found)
+{
+    const uint64_t B = AXBC_SAMPLE_BLOCK, nb = (n + B - 1) / B;
+    *found = 0;
+    if (n == 0) return 0;
+    const double tot = csum[nb - 1];
+    if (isnan(tot) || !(tot >= r)) return n - 1;
+    uint64_t lo = 0, hi = nb;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) / 2;
+        if (csum[mid] >= r) hi = mid;
+        else lo = mid + 1;
+    }
+    const uint64_t b = lo;
+    const double rr = __dsub_rn(r, b > 0 ? csum[b - 1] : 0.0);
+    const uint64_t e = min((b + 1) * B, n);
+    lo = b * B;
+    hi = e;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) / 2;
+        if (local[mid] >= rr) hi = mid;
+        else lo = mid + 1;
+    }
+    *found = 1;
+    return lo < e ? lo : e - 1;
+}
+
+// first index of a wrapping uint32 prefix with prefix >= r, searched run by
+// run (findsample_LOCINT, src/axbc2d.c:2188-2198)
+__device__ uint64_t d_find_u32(const uint32_t *p, const uint32_t *seg_end, uint32_t n_seg, uint32_t r,
+                               int *found)
+{
+    uint32_t start = 0;
+    *found = 0;
+    for (uint32_t k = 0; k < n_seg; k++) {
+        const uint32_t end = seg_end[k];
+        if (end > start && p[end - 1] >= r) {
+            uint32_t lo = start, hi = end;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (p[mid] >= r) hi = mid;
+                else lo = mid + 1;
+            }
+            *found = 1;
+            return lo;
+        }
+        start = end;
+    }
+    return 0;
+}
+
+__device__ bool d_bader(const float *bc, const uint32_t *checks, uint32_t x, uint64_t N, uint32_t c)
+{
+    const double lim = (double)((uint64_t)c * N);
+    for (uint32_t i = 0; i < x; i++) {
+        const double b = checks[i] < N ? (double)bc[checks[i]] : 0.0;
+        if (__ddiv_rn(b, 2.0) < lim) return false;
+    }
+    return true;
+}
+
+// init_rand + the check vertices + the heuristic's set-up draws
+// (src/axbc2d.c:2736-2760, 2793-2795)
+__global__ void k_sampler_init(SamplerState *ss, uint32_t *checks, int64_t seed, int z, uint64_t nbfs,
+                               uint64_t N, uint32_t bader_c, uint32_t nchecks, int W)
+{
+    uint64_t x = (((uint64_t)seed & 0xffffffffULL) << 16) | 0x330EULL;
+    for (uint32_t i = 0; i < nchecks; i++) checks[i] = d_uniform_int(x, (uint32_t)N, 0);
+    uint32_t dist_mix = (uint32_t)z;
+    if (z == 0) (void)d_uniform_int(x, (uint32_t)N, 0);
+    else if (z == 6) dist_mix = d_uniform_int(x, 4, 0);
+    ss->rng = x;
+    ss->ui = 0;
+    ss->nbfs = nbfs < N ? nbfs : N;
+    ss->N = N;
+    ss->z = z;
+    ss->dist_mix = dist_mix;
+    ss->lim = (uint32_t)(N * N);  // int LIMxSAMPLE = N*N, truncated (src/axbc2d.c:2835)
+    ss->bader_c = bader_c;
+    ss->nchecks = nchecks;
+    ss->W = W;
+    ss->done = ss->nbfs == 0;
+    ss->stopped = 0;
+    ss->nrounds = ss->skipped = ss->dropped = ss->te = ss->nrounds_snap = 0;
+    ss->nb = 0;
+    ss->napply = 0;
+    ss->skipped_run = 0;
+}
+
+// Draw the rounds of one batch: up to W accepted pivots.
+__global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const uint32_t *checks,
+                          BatchInfo *bi, double S_lcc)
+{
+    ss->nb = 0;
+    ss->napply = 0;
+    ss->skipped_run = 0;
+    if (ss->done) return;
+    const uint64_t N = ss->N;
+    if (ss->bader_c > 0 && d_bader(D.bc, checks, ss->nchecks, N, ss->bader_c)) {
+        ss->stopped = 1;
+        ss->done = 1;
+        return;
+    }
+    uint64_t x = ss->rng;
+    uint32_t dist_mix = ss->dist_mix;
+    const int z = ss->z;
+    const uint32_t LIM = ss->lim;
+    const bool snap0 = ss->nrounds_snap == 0;
+    const uint64_t nbB = (N + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    double S_bc = 0, S_d = 0;
+    if (!snap0) {
+        if (D.bc_csum) S_bc = D.bc_csum[nbB - 1];
+        if (D.d_csum) S_d = D.d_csum[nbB - 1];
+    }
+    int nb = 0;
+    uint64_t ui = ss->ui, skipped_run = 0, dropped = 0;
+    while (nb < ss->W && ui < ss->nbfs) {
+        uint32_t v0 = 0;
+        double prob = 0;
+        uint32_t BSM = 0;
+        bool good = false;
+        while (!good) {
+            int found;
+            if (BSM > LIM) break;
+            prob = 0;
+            if (dist_mix == 0 || z == 0) {
+                v0 = d_uniform_int(x, (uint32_t)N, 0);
+                prob = __ddiv_rn(1.0, (double)N);
+            } else if (dist_mix == 1 || z == 1) {
+                // high-degree neighbourhood (src/axbc2d.c:2890-2917)
+                const uint32_t r = d_uniform_int(x, D.sum_deg, 0);
+                uint64_t h = d_find_u32(D.deg2p, D.seg_end, D.n_seg, r, &found);
+                if (!found) h = N - 1;
+                const uint32_t dh = D.col[h + 1] - D.col[h];
+                if (dh > 0) {
+                    uint32_t k = 0;
+                    if (dh != 1) k = d_uniform_int(x, dh - 1, 0);
+                    h = D.row[D.col[h] + k];
+                }
+                v0 = (uint32_t)h;
+                prob = __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg);
+            } else if (dist_mix == 2 || z == 2) {
+                // LCC (src/axbc2d.c:2919-2937)
+                const double r = __dmul_rn(d_uniform01(x), S_lcc);
+                uint64_t h = d_hsearch(D.lcc_local, D.lcc_csum, N, r, &found);
+                if (!found) h = N - 1;
+                v0 = (uint32_t)h;
+                prob = __ddiv_rn((double)D.lcc[v0], S_lcc);
+            } else if (dist_mix == 3 || z == 3 || dist_mix == 4 || z == 4 || dist_mix == 5 || z == 5) {
+                const int kind = (dist_mix == 3 || z == 3) ? 3 : (dist_mix == 4 || z == 4) ? 4 : 5;
+                if (snap0) {
+                    v0 = d_uniform_int(x, (uint32_t)N, 0);
+                    prob = __ddiv_rn(1.0, (double)N);
+                } else if (kind == 4) {
+                    // delta of the last pivot (src/axbc2d.c:2970-2991)
+                    const double r = __dmul_rn(d_uniform01(x), S_d);
+                    uint64_t h = d_hsearch(D.d_local, D.d_csum, N, r, &found);
+                    if (!found) h = N - 1;
+                    v0 = (uint32_t)h;
+                    prob = __ddiv_rn((double)D.delta_last[v0], S_d);
+                } else {
+                    // bc (src/axbc2d.c:2941-2969) or 1/(1+bc) (2995-3022)
+                    const double r = __dmul_rn(d_uniform01(x), S_bc);
+                    uint64_t h = d_hsearch(D.bc_local, D.bc_csum, N, r, &found);
+                    if (!found) h = N - 1;
+                    v0 = (uint32_t)h;
+                    if (kind == 3) prob = __ddiv_rn((double)D.bc[v0], S_bc);
+                    else prob = __ddiv_rn(__ddiv_rn(1.0, __dadd_rn((double)D.bc[v0], 1.0)), S_bc);
+                }
+            }
+            if (z == 6) {
+                // mixture probability (src/axbc2d.c:3026-3051)
+                prob = __ddiv_rn(1.0, (double)N);
+                if (snap0) {
+                    prob = __dadd_rn(prob, __ddiv_rn(1.0, (double)N));
+                    prob = __dadd_rn(prob, __ddiv_rn(1.0, (double)N));
+                } else if (v0 < N) {
+                    prob = __dadd_rn(prob, __ddiv_rn((double)D.bc[v0], S_bc));
+                    prob = __dadd_rn(prob, __ddiv_rn((double)D.delta_last[v0], S_d));
+                }
+                if (v0 < N) {
+                    prob = __dadd_rn(prob, __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg));
+                    prob = __dadd_rn(prob, __ddiv_rn((double)D.lcc[v0], S_lcc));
+                    prob = __ddiv_rn(prob, 5.0);
+                }
+                dist_mix = d_uniform_int(x, 2, 0);
+            }
+            if (v0 < N && used[v0]) BSM++;
+            else good = true;
+        }
+        if (BSM > LIM) {  // round dropped (src/axbc2d.c:3072-3077)
+            dropped++;
+            ui++;
+            continue;
+        }
+        if (v0 >= N || D.col[v0 + 1] == D.col[v0]) {  // degree-0 root (3095-3111)
+            skipped_run++;
+            if (v0 < N) used[v0] = 1;
+            ui++;
+            continue;
+        }
+        used[v0] = 1;
+        ss->v0[nb] = v0;
+        ss->p[nb] = prob;
+        ss->skip_before[nb] = skipped_run;
+        bi->root[nb] = v0;
+        bi->p[nb] = prob;
+        skipped_run = 0;
+        nb++;
+        ui++;
+    }
+    ss->rng = x;
+    ss->dist_mix = dist_mix;
+    ss->ui = ui;
+    ss->nb = nb;
+    ss->skipped_run = skipped_run;
+    ss->dropped += dropped;
+}
+
+// After the batch's traversal: replay Bader's test between its pivots, fix
+// how many are applied, and account rounds, skips and traversed edges.
+__global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__restrict__ bc,
+                               const float *__restrict__ mdelta, const uint32_t *__restrict__ seen,
+                               const uint32_t *__restrict__ reach, const uint32_t *__restrict__ checks,
+                               float *b, uint32_t *hist_v, double *hist_p, uint64_t hist_cap)
+{
+    if (ss->done && ss->nb == 0) return;
+    const int nb = ss->nb;
+    const uint64_t N = ss->N;
+    const uint32_t c = ss->bader_c;
+    const double lim = (double)((uint64_t)c * N);
+    int stop = nb;
+    // check-vertex values through the batch, in the order the update applies
+    const uint32_t x = ss->nchecks;
+    const bool track = c > 0;
+    if (track)
+        for (uint32_t i = 0; i < x; i++) b[i] = checks[i] < N ? bc[checks[i]] : 0.0f;
+    for (int s = 0; s < nb; s++) {
+        if (c > 0 && s > 0) {
+            bool sat = true;
+            for (uint32_t i = 0; i < x && sat; i++) {
+                const float bv = track ? b[i] : 0.0f;
+                if (__ddiv_rn((double)bv, 2.0) < lim) sat = false;
+            }
+            if (sat) {
+                stop = s;
+                break;
+            }
+        }
+        if (!track) continue;
+        const uint32_t r = bi->root[s];
+        const uint32_t rr = reach[r];
+        const uint32_t all = (bi->H == 1 ? (uint32_t)bi->rsum[s] : 0u) + rr;
+        const unsigned long long nvt = bi->nvis[s] + all;
+        const double p = bi->p[s];
+        for (uint32_t i = 0; i < x; i++) {
+            const uint32_t v = checks[i];
+            if (v >= N) continue;
+            if (v == r) {
+                if (rr > 0) b[i] = __fadd_rn(b[i], bc_root_term(rr, nvt));
+                continue;
+            }
+            const float dv = ((seen[v] >> s) & 1u) ? mdelta[(uint64_t)v * AXBC_W + s]
+                                                   : __uint2float_rn(reach[v]);
+            if (dv == 0.0f && p > 0.0) continue;
+            b[i] = __fadd_rn(b[i], bc_term(dv, rr, p));
+        }
+    }
+    bi->napply = stop;
+    ss->napply = stop;
+    for (int s = 0; s < stop; s++) {
+        if (ss->nrounds < hist_cap) {
+            hist_v[ss->nrounds] = ss->v0[s];
+            hist_p[ss->nrounds] = ss->p[s];
+        }
+        ss->nrounds++;
+        ss->skipped += ss->skip_before[s];
+        ss->te += 2 * bi->te[s];
+    }
+    if (stop < nb) {
+        ss->stopped = 1;
+        ss->done = 1;
+    } else {
+        if (ss->skipped_run) {
+            bool sat = false;
+            if (c > 0 && nb > 0) {
+                sat = true;
+                for (uint32_t i = 0; i < x && sat; i++) {
+                    const float bv = track ? b[i] : 0.0f;
+                    if (__ddiv_rn((double)bv, 2.0) < lim) sat = false;
+                }
+            }
+            if (sat) {
+                ss->stopped = 1;
+                ss->done = 1;
+            } else {
+                ss->skipped += ss->skipped_run;
+            }
+        }
+        if (ss->ui >= ss->nbfs) ss->done = 1;
+    }
+    ss->nrounds_snap = ss->nrounds;
+}
+
+static int ensure_sampler(axbc_ctx *c, uint32_t nchecks)
+{
+    const uint64_t n = c->g->n;
+    TRY(axbc_ensure_batch(c));
+    if (!c->ss) {
+        TRY(axbc_dalloc((void **)&c->ss, sizeof(SamplerState), &c->bytes));
+        CU(cudaMallocHost((void **)&c->ss_host, sizeof(SamplerState)));
+        TRY(axbc_dalloc((void **)&c->used, n, &c->bytes));
+        const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+        TRY(axbc_dalloc((void **)&c->dyn_local, n * 8, &c->bytes));
+        TRY(axbc_dalloc((void **)&c->dyn_csum, nb * 8, &c->bytes));
+        TRY(axbc_dalloc((void **)&c->dyn_local2, n * 8, &c->bytes));
+        TRY(axbc_dalloc((void **)&c->dyn_csum2, nb * 8, &c->bytes));
+    }
+    if (!c->checks || nchecks > c->nchecks_cap) {
+        axbc_dfree(c->checks);
+        axbc_dfree(c->checkval);
+        TRY(axbc_dalloc((void **)&c->checks, (nchecks + 1) * 4, &c->bytes));
+        TRY(axbc_dalloc((void **)&c->checkval, (nchecks + 1) * 4, &c->bytes));
+        c->nchecks_cap = nchecks;
+    }
+    return AXBC_OK;
+}
+
+extern "C" int axbc_run_sampled(axbc_ctx *c, const axbc_run_params *prm, axbc_run_result *res)
+{
+    CHECK_ARG(c && prm && res, "axbc_run_sampled: null argument");
+    axbc_graph *g = c->g;
+    const uint64_t n = g->n;
+    CHECK_ARG(prm->z >= 0 && prm->z <= 6, "axbc_run_sampled: heuristic must be in [0,6]");
+    CHECK_ARG(prm->H == 0 || prm->H == 1, "axbc_run_sampled: H must be 0 or 1");
+    CHECK_ARG(prm->batch_width >= 1 && prm->batch_width <= AXBC_MAX_BATCH,
+              "axbc_run_sampled: batch_width must be in [1, 32]");
+    CHECK_ARG(prm->nchecks <= n, "axbc_run_sampled: more check vertices than vertices");
+    TRY(ensure_sampler(c, prm->nchecks));
+    cudaStream_t s = c->stream;
+    const int z = prm->z;
+    if (z == 1 || z == 6) TRY(axbc_build_deg_dist(g, s));
+    if (z == 2 || z == 6) TRY(axbc_build_lcc(g, s));
+
+    const uint64_t nbfs = prm->nbfs < n ? prm->nbfs : n;
+    uint32_t *hist_v = nullptr;
+    double *hist_p = nullptr;
+    TRY(axbc_dalloc((void **)&hist_v, (nbfs + 1) * 4, nullptr));
+    TRY(axbc_dalloc((void **)&hist_p, (nbfs + 1) * 8, nullptr));
+
+    CU(cudaMemsetAsync(c->bc, 0, n * 4, s));
+    CU(cudaMemsetAsync(c->delta_last, 0, n * 4, s));
+    CU(cudaMemsetAsync(c->used, 0, n, s));
+    {
+        ProfScope ps(c, KP_SAMPLER, 0);
+        k_sampler_init<<<1, 1, 0, s>>>(c->ss, c->checks, prm->seed, z, prm->nbfs, n,
+                                       (uint32_t)prm->bader_c, prm->nchecks, prm->batch_width);
+    }
+    CU_LAUNCH("k_sampler_init");
+
+    SamplerDists D;
+    memset(&D, 0, sizeof(D));
+    D.col = g->fwd.col;
+    D.row = g->fwd.row;
+    D.deg2p = g->deg2p;
+    D.seg_end = g->seg_end;
+    D.sdn = g->sdn;
+    D.n_seg = g->n_seg;
+    D.sum_deg = g->sum_deg;
+    D.lcc = g->lcc;
+    D.lcc_local = g->lcc_local;
+    D.lcc_csum = g->lcc_csum;
+    D.bc = c->bc;
+    D.delta_last = c->delta_last;
+    const bool dyn_bc = z == 3 || z == 5 || z == 6;
+    const bool dyn_d = z == 4 || z == 6;
+    if (dyn_bc) {
+        D.bc_local = c->dyn_local;
+        D.bc_csum = c->dyn_csum;
+    }
+    if (dyn_d) {
+        D.d_local = c->dyn_local2;
+        D.d_csum = c->dyn_csum2;
+    }
+    const uint64_t nbB = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    const unsigned hb = (unsigned)((nbB + 127) / 128);
+    int batches = 0;
+    for (;;) {
+        if (dyn_bc) {
+            ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
+            k_hprefix_local<<<hb, 128, 0, s>>>(c->bc, n, c->dyn_local, c->dyn_csum, z == 5 ? 1 : 0, c->ss);
+        }
+        if (dyn_bc) {
+            ProfScope ps(c, KP_SAMPLER, 0);
+            k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum, nbB, c->ss);
+        }
+        if (dyn_d) {
+            ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
+            k_hprefix_local<<<hb, 128, 0, s>>>(c->delta_last, n, c->dyn_local2, c->dyn_csum2, 0, c->ss);
+        }
+        if (dyn_d) {
+            ProfScope ps(c, KP_SAMPLER, 0);
+            k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum2, nbB, c->ss);
+        }
+        {
+            ProfScope ps(c, KP_SAMPLER, 0);
+            k_sampler<<<1, 1, 0, s>>>(c->ss, D, c->used, c->checks, c->bi, g->S_lcc);
+        }
+        CU_LAUNCH("k_sampler");
+        CU(cudaMemcpyAsync(c->ss_host, c->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        const int nb = c->ss_host->nb;
+        if (c->ss_host->done && nb == 0 && c->ss_host->skipped_run == 0) break;
+        if (nb > 0) {
+            TRY(axbc_batch_traverse(c, nb, prm->H));
+            batches++;
+        }
+        {
+            ProfScope ps(c, KP_SAMPLER, 0);
+            k_sampler_post<<<1, 1, 0, s>>>(c->ss, c->bi, c->bc, c->mdelta, c->seen, g->reach,
+                                           c->checks, c->checkval, hist_v, hist_p, nbfs + 1);
+        }
+        CU_LAUNCH("k_sampler_post");
+        if (nb > 0) TRY(axbc_batch_apply(c));
+    }
+    CU(cudaMemcpyAsync(c->ss_host, c->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    const SamplerState &S = *c->ss_host;
+    res->nrounds = S.nrounds;
+    res->skipped = S.skipped;
+    res->dropped = S.dropped;
+    res->rounds = S.ui;
+    res->te = S.te;
+    res->stopped = S.stopped;
+    res->batches = batches;
+    const uint64_t k = std::min<uint64_t>(S.nrounds, nbfs + 1);
+    c->run_pivots.resize(k);
+    c->run_probs.resize(k);
+    c->run_checks.resize(prm->nchecks);
+    if (k) {
+        CU(cudaMemcpy(c->run_pivots.data(), hist_v, k * 4, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(c->run_probs.data(), hist_p, k * 8, cudaMemcpyDeviceToHost));
+    }
+    if (prm->nchecks)
+        CU(cudaMemcpy(c->run_checks.data(), c->checks, prm->nchecks * 4, cudaMemcpyDeviceToHost));
+    axbc_dfree(hist_v);
+    axbc_dfree(hist_p);
+    return AXBC_OK;
+}
+
+extern "C" int axbc_get_pivots(const axbc_ctx *c, uint32_t *v0, double *p, uint64_t cap,
+                               uint64_t *count)
+{
+    CHECK_ARG(c, "axbc_get_pivots: null context");
+    const uint64_t k = std::min<uint64_t>(cap, c->run_pivots.size());
+    for (uint64_t i = 0; i < k; i++) {
+        if (v0) v0[i] = c->run_pivots[i];
+        if (p) p[i] = c->run_probs[i];
+    }
+    if (count) *count = c->run_pivots.size();
+    return AXBC_OK;
+}
+
+extern "C" int axbc_get_checks(const axbc_ctx *c, uint32_t *checks, uint32_t cap)
+{
+    CHECK_ARG(c && checks, "axbc_get_checks: null argument");
+    for (uint32_t i = 0; i < cap && i < c->run_checks.size(); i++) checks[i] = c->run_checks[i];
+    return AXBC_OK;
+}

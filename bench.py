@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""Benchmark: BC traversed-edges/s (forward + backward) on GB300.
+
+Workload (the headline configuration): Kronecker/R-MAT scale 23, edgefactor 16,
+undirected, heuristic 3 (bc-based dynamic sampling), 1024 pivots per step in
+batches of 32, Bader test off.  One step is one sampled BC run of 1024 pivots:
+device sampling, the batched forward/backward passes and the bc updates.  TE
+per pivot = 2 * degree sum of the vertices it reaches (Graph500 counting).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the oracle (oracle/, a C restatement of the reference
+path; the reference itself cannot be built here) on the host cores with
+OpenMP, on a bounded pivot sample of the same graph and pivot list.
+
+Input generation (device R-MAT + CSC build) is set-up and is not timed.
+The graph (~1.1 GB of adjacency) is larger than L2, so no L2 flush is needed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=23)
+    ap.add_argument("--edgefactor", type=int, default=16)
+    ap.add_argument("--pivots", type=int, default=1024, help="pivots per step")
+    ap.add_argument("--width", type=int, default=32, help="batch width")
+    ap.add_argument("--z", type=int, default=3, help="sampling heuristic")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target CPU time of the oracle baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = str(index)
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9 and parts[0] == self.index:
+                self.rows.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = sorted(float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit())
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if r[5 + i].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(self.rows), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_for(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` from a committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        ent = t.get(workload, {}).get(kernel)
+        return None if ent is None else float(ent["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def oracle_sample(g_csc, pivots, probs, seconds, threads):
+    """Time the oracle (OpenMP over pivots) on a bounded pivot sample."""
+    import numpy as np
+    import oracle
+    oracle.build()
+    g = oracle.CSC(*g_csc)
+    # size the sample: one pivot per thread first, then scale to the budget
+    k0 = min(len(pivots), threads)
+    t0 = time.perf_counter()
+    _, te0 = oracle.bc_pivots_omp(g, pivots[:k0], probs[:k0], 0, threads)
+    dt0 = time.perf_counter() - t0
+    k = k0
+    if dt0 < seconds:
+        k = int(min(len(pivots), max(k0, k0 * (seconds / max(dt0, 1e-3)))))
+        k = max(threads, (k // threads) * threads) if k >= threads else k
+    if k == k0:
+        return te0 / dt0, k0, dt0
+    t0 = time.perf_counter()
+    _, te = oracle.bc_pivots_omp(g, pivots[:k], probs[:k], 0, threads)
+    dt = time.perf_counter() - t0
+    return te / dt, k, dt
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    import numpy as np
+
+    workload = (f"kronecker-s{args.scale}-ef{args.edgefactor} undirected, -z {args.z} "
+                f"-N {args.pivots} -c 0, batch width {args.width}")
+    metric = "BC traversed-edges/s (fwd+bwd)"
+    config = {"workload": workload, "scale": args.scale, "edgefactor": args.edgefactor,
+              "pivots_per_step": args.pivots, "batch_width": args.width,
+              "heuristic": args.z, "bader_c": 0,
+              "l2": "inputs larger than L2 (adjacency ~4*m bytes, no flush)",
+              "parallelism": f"pivot-sharded replicas x{world}"}
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import axbc_gb300 as ax
+    ax.lib()
+
+    G = ax.Graph.rmat(args.scale, args.edgefactor, seed=23)
+    stream = torch.cuda.Stream()
+    ctx = ax.Context(G, stream=stream.cuda_stream)
+
+    def step(seed):
+        return ctx.run_sampled(z=args.z, nbfs=args.pivots, bader_c=0, nchecks=1, H=0, seed=seed,
+                               W=args.width)
+
+    seed = 4343543 + rank
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # the graph and the pivot list of the gb300 arm; the oracle is timed
+        first = step(seed)
+        csc = G.csc()
+        piv, pr = first["pivots"], first["probs"]
+        threads = cpu_threads()
+        vals = []
+        for _ in range(args.warmup):
+            oracle_sample(csc, piv, pr, args.cpu_seconds / 3, threads)
+        t_all = time.perf_counter()
+        ks = []
+        for _ in range(args.steps):
+            v, k, dt = oracle_sample(csc, piv, pr, args.cpu_seconds / 3, threads)
+            vals.append(v)
+            ks.append(k)
+        wall = time.perf_counter() - t_all
+        val = float(np.mean(vals))
+        out = {"metric": metric, "value": val, "unit": "TE/s", "n_gpus": 1, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": wall * 1000 / max(args.steps, 1),
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "u32 path counts, f32 dependencies/bc", "data": "synthetic",
+               "config": config, "impl": "reference",
+               "cpu_baseline": {"value": val, "unit": "TE/s", "cores": threads, "kind": "port",
+                                "sample": f"{ks[0]} pivots of the step's pivot list per step, "
+                                          "OpenMP over pivots (oracle/ C restatement; the "
+                                          "reference needs MPI and does not build here)"},
+               "e2e": {"value": val, "unit": "TE/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
+        return
+
+    # ---------------------------------------------------------------- gb300
+    for _ in range(args.warmup):
+        step(seed)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local]
+                          if "CUDA_VISIBLE_DEVICES" in os.environ else local)
+    clocks.start()
+    ctx.profile(True)
+    l0 = ctx.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    te = 0
+    last = None
+    for _ in range(args.steps):
+        last = step(seed)
+        te += last["te"]
+    if world > 1:
+        # the one exchange of the sharded path: sum the ranks' bc
+        bc_t = torch.empty(G.n, dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            dist.all_reduce(bc_t)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    clk = clocks.stop()
+    t = ev0.elapsed_time(ev1) / 1000.0
+    te_all = te
+    if world > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+        tv = torch.tensor([te], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tv)
+        te_all = float(tv.item())
+    value = te_all / t
+
+    # roofline of the dominant kernel kind
+    peak, peak_kind = peaks()
+    kind = max(prof, key=lambda k: prof[k][0])
+    ms, cnt, by = prof[kind]
+    achieved = (by / (ms / 1000.0)) / 1e9 if ms > 0 else 0.0
+    kernel = ax.PROF_KERNELS[kind]
+    traffic = traffic_for(kernel, workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
+                "launches": cnt, "avg_launch_ms": ms / max(cnt, 1),
+                "algorithmic_bytes_per_launch": by / max(cnt, 1),
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "share_of_kernel_time": ms / max(sum(v[0] for v in prof.values()), 1e-9),
+                "kernel_ms": {k: round(v[0], 3) for k, v in prof.items() if v[1]}}
+
+    # e2e: the same pivots through the host-buffer C ABI (pinned inputs/outputs)
+    piv = last["pivots"]
+    pr = last["probs"]
+    nb = (len(piv) + args.width - 1) // args.width
+    h_piv = torch.from_numpy(piv.astype(np.uint32).view(np.int32)).pin_memory()
+    h_pr = torch.from_numpy(pr.astype(np.float64)).pin_memory()
+    h_bc = torch.empty(G.n, dtype=torch.float32).pin_memory()
+    piv_np, pr_np, bc_np = h_piv.numpy().view(np.uint32), h_pr.numpy(), h_bc.numpy()
+
+    def e2e_step():
+        ctx.reset()
+        tot = 0
+        for b in range(nb):
+            sl = slice(b * args.width, min(len(piv), (b + 1) * args.width))
+            st = ctx.run_batch(piv_np[sl], pr_np[sl], 0)
+            tot += sum(s["te"] for s in st)
+        import ctypes
+        ax._check(ax.lib().axbc_get_bc(ctx._h, bc_np.ctypes.data_as(ctypes.c_void_p)))
+        return tot
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_te = 0
+    for _ in range(args.steps):
+        e2e_te += e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    e2e = {"value": e2e_te * world / e2e_t, "unit": "TE/s",
+           "h2d_bytes_per_step": int(len(piv) * 12), "d2h_bytes_per_step": int(G.n * 4),
+           "api": "axbc_run_batch (host pivot/p arrays) + axbc_get_bc (pinned host bc)"}
+
+    # the plain form (one pivot per launch sequence, host-driven levels) on a
+    # sample of the same pivots: the denominator of the batched form's speed-up
+    k_plain = min(len(piv), 64)
+    ctx.reset()
+    torch.cuda.synchronize()
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev2.record(stream)
+    plain_te = 0
+    for v0, p0 in zip(piv[:k_plain], pr[:k_plain]):
+        plain_te += ctx.run_pivot(int(v0), float(p0), 0)["te"]
+    ev3.record(stream)
+    torch.cuda.synchronize()
+    plain_t = ev2.elapsed_time(ev3) / 1000.0
+    plain = {"value": plain_te / plain_t, "unit": "TE/s", "pivots": k_plain,
+             "speedup_of_value": value / world / (plain_te / plain_t)}
+
+    out = {"metric": metric, "value": value, "unit": "TE/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000 / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "u32 path counts, f32 dependencies/bc", "data": "synthetic",
+           "config": config, "e2e": e2e, "roofline": roofline, "clocks": clk,
+           "gpu_launches": int(launches), "plain_form": plain,
+           "te_per_step": te_all / args.steps, "pivots_applied_per_step": int(last["nrounds"])}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        csc = G.csc()
+        threads = cpu_threads()
+        v, k, dt = oracle_sample(csc, piv, pr, args.cpu_seconds, threads)
+        out["cpu_baseline"] = {"value": v, "unit": "TE/s", "cores": threads, "kind": "port",
+                               "sample": f"{k} pivots of the step's pivot list in {dt:.1f} s, "
+                                         "OpenMP over pivots (oracle/ C restatement)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

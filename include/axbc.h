@@ -1,0 +1,215 @@
+/*
+ * axbc_gb300 -- GB300-native sampled-Brandes betweenness centrality.
+ *
+ * C ABI of libaxbc_gb300.so.  Plain pointers and sizes only; every call
+ * returns an axbc status (0 = AXBC_OK) and never exits the process.  Host
+ * buffers belong to the caller, device buffers to the library.  A graph and
+ * the contexts built on it live on the CUDA device that was current when the
+ * graph was created.  Calls on different contexts may come from different
+ * host threads; calls on one context must be serialised by the caller.
+ *
+ * Reference: fvella/axbc, whose host driver (src/axbc2d.c) calls its CUDA
+ * file (src/cuda_kernels.cu) through the extern "C" table of src/bc2d.h:
+ * 136-190.  Each entry point below names the reference interface it replaces.
+ * The reference's own names and signatures are also exported, unchanged, by
+ * the compatibility layer declared in axbc_compat.h.
+ */
+#ifndef AXBC_H
+#define AXBC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    AXBC_OK = 0,
+    AXBC_ERR_INVALID = 1,    /* bad argument (null pointer, vertex >= n, ...) */
+    AXBC_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    AXBC_ERR_NOMEM = 3,      /* device or host allocation failed */
+    AXBC_ERR_TIMEOUT = 4,    /* a bounded device-side wait gave up */
+    AXBC_ERR_RANGE = 5,      /* a size exceeds a documented limit */
+    AXBC_ERR_STATE = 6,      /* call out of order (e.g. no batch pending) */
+    AXBC_ERR_BUSY = 7        /* serving: admission refused for lack of memory */
+};
+
+/* Batch width of the multi-source pass (sources per warp bitmask). */
+#define AXBC_MAX_BATCH 32
+
+typedef struct axbc_graph axbc_graph;
+typedef struct axbc_ctx axbc_ctx;
+
+const char *axbc_status_str(int status);
+/* Text of the last error raised on the calling host thread. */
+const char *axbc_last_error(void);
+/* Library version string. */
+const char *axbc_version(void);
+
+/* ---------------------------------------------------------------- graphs */
+
+/* Edge list (pairs of uint64 vertex ids < n) -> the reference's CSC, on the
+ * host: mirror if `undirected`, then norm_graph, degree_reduction when H == 1,
+ * norm_graph, build_csc.  Replaces read_graph/gen_graph's post-processing in
+ * src/axbc2d.c:333-351, 695-907, 2551-2622.  The returned arrays are
+ * allocated by the library; release them with axbc_host_free.
+ * *col: n+1 offsets; *row: *m neighbour ids; *reach: n removed-leaf counts. */
+int axbc_edges_to_csc(const uint64_t *edges, uint64_t nedges, uint64_t n, int undirected,
+                      int H, uint32_t **col, uint32_t **row, uint64_t *m, uint32_t **reach,
+                      uint64_t *removed_leaves);
+void axbc_host_free(void *p);
+
+/* Read an edge-list text file the way read_graph (src/axbc2d.c:356-445)
+ * does: '#' lines are comments, other lines "u v".  Returns the edges (uint64
+ * pairs, library-allocated) without mirroring. */
+int axbc_read_edge_file(const char *path, uint64_t n, uint64_t **edges, uint64_t *nedges);
+
+/* Upload a CSC graph (reference layout: column c lists the rows r of the
+ * edges (r,c), ascending) to the current device.  `reach` may be NULL (all
+ * zero).  Replaces initcuda + init_bc_1degree_device (src/cuda_kernels.cu:
+ * 1558-1600, 1515-1519). */
+int axbc_graph_create(const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
+                      const uint32_t *reach, axbc_graph **g);
+
+/* Synthetic inputs generated and built on the device: an R-MAT graph of
+ * 2^scale vertices and edgefactor*2^scale generated edges (initiator
+ * A,B,C = .57,.19,.19), vertex ids scrambled, self-loops and duplicates
+ * removed, mirrored unless `directed`.  H == 1 applies the one-degree
+ * reduction.  (The reference generates with the Graph500 generator,
+ * src/axbc2d.c:518-527; this generator is the library's own.) */
+int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed, int directed, int H,
+                             axbc_graph **g);
+/* side x side 4-neighbour grid; each grid edge dropped with probability
+ * drop_prob; floor(longrange_frac * kept_edges) extra random edges; mirrored. */
+int axbc_graph_generate_grid(uint32_t side, double drop_prob, double longrange_frac,
+                             uint64_t seed, axbc_graph **g);
+
+int axbc_graph_destroy(axbc_graph *g);
+/* n, m, device bytes held, 1 if the adjacency is symmetric */
+int axbc_graph_info(const axbc_graph *g, uint64_t *n, uint64_t *m, uint64_t *bytes,
+                    int *symmetric);
+/* Degrees (get_deg, src/cuda_kernels.cu:1452-1454), CSC arrays, reach. */
+int axbc_graph_get_deg(const axbc_graph *g, uint32_t *deg_host);
+int axbc_graph_get_csc(const axbc_graph *g, uint32_t *col_host, uint32_t *row_host,
+                       uint32_t *reach_host);
+
+/* -------------------------------------------------------------- contexts */
+
+/* A context holds the BC state of one computation on one graph: bc (float),
+ * per-pivot state, the multi-source batch state and the sampler.  `stream`
+ * is a cudaStream_t or NULL for a stream of its own. */
+int axbc_ctx_create(axbc_graph *g, void *stream, axbc_ctx **ctx);
+int axbc_ctx_destroy(axbc_ctx *ctx);
+/* bc = 0, sampler state cleared */
+int axbc_ctx_reset(axbc_ctx *ctx);
+/* device bytes held by the context */
+int axbc_ctx_bytes(const axbc_ctx *ctx, uint64_t *bytes);
+
+/* Tuning knobs (autotuner output).  push_factor: a forward level pushes from
+ * the frontier when frontier_edges * push_factor < unvisited_edges, else it
+ * pulls into unvisited vertices.  Defaults are built in. */
+int axbc_ctx_set_tuning(axbc_ctx *ctx, double push_factor_single, double push_factor_batch);
+
+/* ---- per-pivot (plain form) ----
+ * One Brandes pass from v0 with selection probability p: forward BFS with
+ * uint32 path counts, backward float dependencies, bc update, exactly as
+ * setcuda + bc_func_mono + update_bc_cuda (src/cuda_kernels.cu:1532-1554,
+ * src/axbc2d.c:1514-1659, src/cuda_kernels.cu:289-302).  H == 1 adds the
+ * reach sum of pre_update_bc_cuda (src/cuda_kernels.cu:358-373).  The host
+ * drives one launch sequence per BFS level. */
+typedef struct {
+    uint64_t nvisited;  /* vertices reached, root included */
+    uint64_t all;       /* reach total added in the root term */
+    uint64_t te;        /* traversed edges: 2 * degree sum of reached vertices */
+    int32_t levels;     /* first empty BFS level */
+    int32_t pad;
+} axbc_pivot_stats;
+
+int axbc_run_pivot(axbc_ctx *ctx, uint32_t v0, double p, int H, axbc_pivot_stats *stats);
+
+/* ---- batched (multi-source) form ----
+ * k <= AXBC_MAX_BATCH pivots in one multi-source pass (one bit per pivot in a
+ * 32-bit mask per vertex).  bc receives the pivots' updates in list order,
+ * bit-identical to k calls of axbc_run_pivot.  stats may be NULL. */
+int axbc_run_batch(axbc_ctx *ctx, const uint32_t *v0, const double *p, int k, int H,
+                   axbc_pivot_stats *stats);
+
+/* ---- sampled run (the reference's main loop) ----
+ * Draws pivots with heuristic z (-z 0..6), stops after nbfs rounds (-N) or
+ * when Bader's criterion holds for nchecks check vertices (-c, -x).  Sampling
+ * and the stop test run on the device.  batch_width 1 reproduces the
+ * reference's round sequence; larger widths draw each batch from the
+ * distributions as they stood before it (src/axbc2d.c:2729-3156). */
+typedef struct {
+    int32_t z;            /* heuristic 0..6 */
+    int32_t bader_c;      /* Bader constant; 0 disables the stop test */
+    uint64_t nbfs;        /* round limit (capped at n) */
+    uint32_t nchecks;     /* check vertices */
+    int32_t H;            /* 1: one-degree reach terms */
+    int64_t seed;         /* srand48 seed; 4343543 is the reference default */
+    int32_t batch_width;  /* 1..AXBC_MAX_BATCH */
+    int32_t pad;
+} axbc_run_params;
+
+typedef struct {
+    uint64_t nrounds;     /* pivots applied */
+    uint64_t skipped;     /* degree-0 draws */
+    uint64_t dropped;     /* rounds lost to the bad-sample limit */
+    uint64_t rounds;      /* round counter at the end */
+    uint64_t te;          /* traversed edges of the applied pivots */
+    int32_t stopped;      /* 1 if Bader's criterion ended the run */
+    int32_t batches;      /* batches launched */
+} axbc_run_result;
+
+int axbc_run_sampled(axbc_ctx *ctx, const axbc_run_params *prm, axbc_run_result *res);
+/* The pivots applied by the last sampled run, in order, with their p. */
+int axbc_get_pivots(const axbc_ctx *ctx, uint32_t *v0, double *p, uint64_t cap,
+                    uint64_t *count);
+/* The check vertices drawn by the last sampled run. */
+int axbc_get_checks(const axbc_ctx *ctx, uint32_t *checks, uint32_t cap);
+
+/* ---- results ---- */
+/* get_bc (src/cuda_kernels.cu:1461-1463): n floats. */
+int axbc_get_bc(axbc_ctx *ctx, float *bc_host);
+/* get_delta (:1465-1467): the last applied pivot's dependencies, n floats. */
+int axbc_get_delta(axbc_ctx *ctx, float *delta_host);
+/* The last plain pivot's path counts and levels (get_sigma / get_lvl). */
+int axbc_get_sigma(axbc_ctx *ctx, uint32_t *sigma_host);
+int axbc_get_levels(axbc_ctx *ctx, int32_t *lvl_host);
+/* One source of the last batch: its path counts, depths (-1 unreached) and
+ * dependencies. */
+int axbc_get_batch_source(axbc_ctx *ctx, int source, uint32_t *sigma_host, int32_t *lvl_host,
+                          float *delta_host);
+/* Device pointer of bc (n floats) for callers that keep results on the GPU. */
+int axbc_bc_device_ptr(axbc_ctx *ctx, float **bc_dev);
+/* Wait for all work of the context. */
+int axbc_ctx_sync(axbc_ctx *ctx);
+
+/* ---- profiling ----
+ * With profiling on, the library records a CUDA event pair on the context's
+ * stream around each of its kernel launches and the algorithmic bytes of the
+ * launch (the traversed-edge byte model: per traversed edge 4/W+4 bytes
+ * forward and 4/W+8 backward for a batch of W pivots, 8 and 12 for one pivot;
+ * 20 bytes per vertex per pivot for the update).  Kinds:
+ * 0 batched forward push, 1 batched forward pull, 2 level bookkeeping,
+ * 3 batched backward, 4 heavy-vertex combine, 5 bc update, 6 sampler,
+ * 7 plain forward, 8 plain backward, 9 plain other. */
+#define AXBC_PROF_KINDS 10
+int axbc_ctx_profile(axbc_ctx *ctx, int enable);
+/* per kind: total milliseconds, launches, algorithmic bytes; clears the records */
+int axbc_ctx_profile_read(axbc_ctx *ctx, double *ms, uint64_t *count, double *bytes, int nkinds);
+/* kernels launched by this context since it was created */
+int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
+
+/* ---- static pivot distributions (device) ---- */
+/* (uint32)deg^2, neighbour-degree sums (sum_deg_neigh_func, src/axbc2d.c:
+ * 1758-1845) and local clustering coefficients (lcc_func, :1847-1935). */
+int axbc_graph_degree2(axbc_graph *g, uint32_t *out_host);
+int axbc_graph_sum_deg_neigh(axbc_graph *g, uint32_t *out_host);
+int axbc_graph_lcc(axbc_graph *g, float *out_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AXBC_H */
