@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the oracle baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no e2e pass")
+    ap.add_argument("--skip-plain", action="store_true", help="profiling runs: no plain pass")
     return ap.parse_args()
 
 
@@ -285,7 +287,7 @@ def main():
     h_bc = torch.empty(G.n, dtype=torch.float32).pin_memory()
     piv_np, pr_np, bc_np = h_piv.numpy().view(np.uint32), h_pr.numpy(), h_bc.numpy()
 
-    def e2e_step():
+    def e2e_step_():
         ctx.reset()
         tot = 0
         for b in range(nb):
@@ -296,21 +298,23 @@ def main():
         ax._check(ax.lib().axbc_get_bc(ctx._h, bc_np.ctypes.data_as(ctypes.c_void_p)))
         return tot
 
-    e2e_step()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_te = 0
-    for _ in range(args.steps):
-        e2e_te += e2e_step()
-    torch.cuda.synchronize()
-    e2e_t = time.perf_counter() - t0
-    e2e = {"value": e2e_te * world / e2e_t, "unit": "TE/s",
-           "h2d_bytes_per_step": int(len(piv) * 12), "d2h_bytes_per_step": int(G.n * 4),
-           "api": "axbc_run_batch (host pivot/p arrays) + axbc_get_bc (pinned host bc)"}
+    e2e = None
+    if not args.skip_e2e:
+        e2e_step_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_te = 0
+        for _ in range(args.steps):
+            e2e_te += e2e_step_()
+        torch.cuda.synchronize()
+        e2e_t = time.perf_counter() - t0
+        e2e = {"value": e2e_te * world / e2e_t, "unit": "TE/s",
+               "h2d_bytes_per_step": int(len(piv) * 12), "d2h_bytes_per_step": int(G.n * 4),
+               "api": "axbc_run_batch (host pivot/p arrays) + axbc_get_bc (pinned host bc)"}
 
     # the plain form (one pivot per launch sequence, host-driven levels) on a
     # sample of the same pivots: the denominator of the batched form's speed-up
-    k_plain = min(len(piv), 64)
+    k_plain = 0 if args.skip_plain else min(len(piv), 64)
     ctx.reset()
     torch.cuda.synchronize()
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -321,8 +325,10 @@ def main():
     ev3.record(stream)
     torch.cuda.synchronize()
     plain_t = ev2.elapsed_time(ev3) / 1000.0
-    plain = {"value": plain_te / plain_t, "unit": "TE/s", "pivots": k_plain,
-             "speedup_of_value": value / world / (plain_te / plain_t)}
+    plain = None
+    if k_plain:
+        plain = {"value": plain_te / plain_t, "unit": "TE/s", "pivots": k_plain,
+                 "speedup_of_value": value / world / (plain_te / plain_t)}
 
     out = {"metric": metric, "value": value, "unit": "TE/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000 / args.steps,
