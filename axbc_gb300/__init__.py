@@ -37,6 +37,12 @@ class RunParams(C.Structure):
                 ("batch_width", C.c_int32), ("pad", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("push_factor_single", C.c_double), ("push_factor_batch", C.c_double),
+                ("batch_width", C.c_int32), ("pad", C.c_int32), ("batch_te_per_s", C.c_double),
+                ("plain_te_per_s", C.c_double)]
+
+
 class RunResult(C.Structure):
     _fields_ = [("nrounds", C.c_uint64), ("skipped", C.c_uint64), ("dropped", C.c_uint64),
                 ("rounds", C.c_uint64), ("te", C.c_uint64), ("stopped", C.c_int32),
@@ -89,6 +95,9 @@ _SIGS = {
     "axbc_ctx_profile": (C.c_int, [_P, C.c_int]),
     "axbc_ctx_profile_read": (C.c_int, [_P, _P, _P, _P, C.c_int]),
     "axbc_ctx_launches": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "axbc_autotune": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(Tuning)]),
+    "axbc_selftest_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
+                                         C.POINTER(C.c_uint64)]),
 }
 
 PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bwd",
@@ -320,6 +329,15 @@ class Context:
     def sync(self):
         _check(lib().axbc_ctx_sync(self._h))
 
+    def autotune(self, pivots, H=0):
+        """Pick direction-switch factors and batch width on these pivots (resets bc)."""
+        v = np.ascontiguousarray(pivots, dtype=np.uint32)
+        t = Tuning()
+        _check(lib().axbc_autotune(self._h, _ptr(v), len(v), H, C.byref(t)))
+        return dict(push_factor_single=t.push_factor_single,
+                    push_factor_batch=t.push_factor_batch, batch_width=t.batch_width,
+                    batch_te_per_s=t.batch_te_per_s, plain_te_per_s=t.plain_te_per_s)
+
     def profile(self, enable=True):
         """Record CUDA events around every kernel launch of this context."""
         _check(lib().axbc_ctx_profile(self._h, int(enable)))
@@ -349,6 +367,13 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def selftest_division(n=1 << 26, seed=1):
+    """(mismatches, exact-path count) of the update's division fast path."""
+    bad, slow = C.c_uint64(), C.c_uint64()
+    _check(lib().axbc_selftest_division(n, seed, C.byref(bad), C.byref(slow)))
+    return bad.value, slow.value
 
 
 def exported_symbols():

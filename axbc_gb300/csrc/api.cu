@@ -171,6 +171,8 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     for (uint32_t *p : c->fmask) axbc_dfree(p);
     axbc_dfree(c->msigma);
     axbc_dfree(c->mdelta);
+    axbc_dfree(c->mq);
+    axbc_dfree(c->task_ctr);
     axbc_dfree(c->mpartial);
     axbc_dfree(c->bi);
     if (c->bi_host) cudaFreeHost(c->bi_host);

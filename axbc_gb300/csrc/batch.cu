@@ -6,6 +6,7 @@
 // counts are integers, and each lane accumulates its dependency sum in the
 // canonical order (32-position chunks summed as a tree in registers, chunks
 // then spans left to right).
+#include <algorithm>
 #include <cstddef>
 #include <vector>
 
@@ -54,9 +55,28 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, u
     }
 }
 
+// ---------------------------------------------------------- task scheduling
+// Work units handed out by an atomic counter: units [0, nhi) are the span
+// items of heavy vertices (largest first), the remaining units cover four
+// light tasks each (light tasks: degree-ordered groups of <= 32 vertices with
+// about one span of adjacency).
+#define LIGHT_PER_UNIT 4
+
+__device__ __forceinline__ uint32_t grab_unit(uint32_t *ctr)
+{
+    uint32_t t = 0;
+    if (lane_id() == 0) t = atomicAdd(ctr, 1u);
+    return __shfl_sync(FULL_MASK, t, 0);
+}
+
+__host__ __device__ __forceinline__ uint64_t n_units(const Adj &a)
+{
+    return a.n_heavy_items + (a.n_ltask + LIGHT_PER_UNIT - 1) / LIGHT_PER_UNIT;
+}
+
 // Forward level L, push from the vertices of depth L-1: for each neighbour u
 // and each pivot s with v at depth L-1 and u unseen, sigma_s[u] += sigma_s[v]
-// and bit s joins u's level-L mask.
+// and bit s joins u's level-L mask.  Atomics are fire-and-forget reductions.
 __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, uint32_t b0,
                                           uint32_t b1, const uint32_t *__restrict__ seen,
                                           uint32_t *fcur, uint32_t *msigma)
@@ -85,43 +105,49 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
 __global__ void __launch_bounds__(BATCH_TPB) k_fwd_push_m(Adj a, const uint32_t *__restrict__ fprev,
                                                           uint32_t *fcur,
                                                           const uint32_t *__restrict__ seen,
-                                                          uint32_t *msigma)
+                                                          uint32_t *msigma, uint32_t *ctr)
 {
     const unsigned lane = lane_id();
-    const uint64_t n = a.n, nblk = (n + 31) / 32, ntask = nblk + a.n_heavy_items;
-    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
-    for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; t < ntask; t += nw) {
-        if (t < nblk) {
-            const uint64_t v_l = t * 32 + lane;
-            uint32_t f_l = 0;
-            if (v_l < n) {
+    const uint64_t nhi = a.n_heavy_items, nu = n_units(a);
+    for (;;) {
+        const uint32_t t = grab_unit(ctr);
+        if (t >= nu) break;
+        if (t < nhi) {
+            const uint32_t v = a.hitem_v[t];
+            const uint32_t f = fprev[v];
+            if (!f) continue;
+            const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
+            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma);
+            continue;
+        }
+        const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
+        for (uint64_t lt = l0; lt < l0 + LIGHT_PER_UNIT && lt < a.n_ltask; lt++) {
+            const uint32_t beg = a.ltask[lt], cnt = a.ltask[lt + 1] - beg;
+            uint32_t v_l = 0, f_l = 0;
+            if (lane < cnt) {
+                v_l = a.order[beg + lane];
                 f_l = fprev[v_l];
-                if (f_l && a.col[v_l + 1] - a.col[v_l] > AXBC_SPAN) f_l = 0;
             }
             unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
             while (act) {
                 const int j = __ffs(act) - 1;
                 act &= act - 1;
-                const uint32_t v = (uint32_t)(t * 32 + j);
+                const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
                 const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
                 push_span(a, v, f, a.col[v], a.col[v + 1], seen, fcur, msigma);
             }
-        } else {
-            const uint64_t h = t - nblk;
-            const uint32_t v = a.hitem_v[h];
-            const uint32_t f = fprev[v];
-            if (!f) continue;
-            const uint32_t b0 = a.col[v] + a.hitem_k[h] * AXBC_SPAN;
-            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma);
         }
     }
 }
 
 // Forward level L, pull into vertex u for the pivots `ns` that have not seen
-// it: sum sigma_s over every in-neighbour at depth L-1 from pivot s.
+// it: sum sigma_s over every in-neighbour at depth L-1 from pivot s.  The
+// positions of a 32-wide chunk are staged in shared memory and their gathers
+// issued eight at a time before any is consumed.
 __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32_t b0, uint32_t b1,
                                               const uint32_t *__restrict__ fprev,
-                                              const uint32_t *__restrict__ msigma, uint32_t &acc)
+                                              const uint32_t *__restrict__ msigma, uint32_t *su,
+                                              uint32_t *sg, uint32_t &acc)
 {
     const unsigned lane = lane_id();
     bool found = false;
@@ -134,16 +160,28 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
             fm = fprev[v] & ns;
         }
         unsigned act = __ballot_sync(FULL_MASK, fm != 0);
+        if (!act) continue;
+        su[lane] = v;
+        sg[lane] = fm;
+        __syncwarp();
         while (act) {
-            const int j = __ffs(act) - 1;
-            act &= act - 1;
-            const uint32_t vj = __shfl_sync(FULL_MASK, v, j);
-            const uint32_t mj = __shfl_sync(FULL_MASK, fm, j);
-            if ((mj >> lane) & 1u) {
-                acc += msigma[row_base(vj) + lane];
-                found = true;
+            uint32_t x[8];
+            bool h[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int j = act ? __ffs(act) - 1 : 0;
+                const bool ok = act != 0;
+                act &= act - 1;
+                h[q] = ok && ((sg[j] >> lane) & 1u);
+                x[q] = h[q] ? msigma[row_base(su[j]) + lane] : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                acc += x[q];
+                found |= h[q];
             }
         }
+        __syncwarp();
     }
     return __ballot_sync(FULL_MASK, found);
 }
@@ -152,43 +190,49 @@ __global__ void __launch_bounds__(BATCH_TPB) k_fwd_pull_m(Adj rv, uint32_t srcma
                                                           const uint32_t *__restrict__ fprev,
                                                           uint32_t *fcur,
                                                           const uint32_t *__restrict__ seen,
-                                                          uint32_t *msigma)
+                                                          uint32_t *msigma, uint32_t *ctr)
 {
+    __shared__ uint32_t s_u[BATCH_TPB], s_g[BATCH_TPB];
     const unsigned lane = lane_id();
-    const uint64_t n = rv.n, nblk = (n + 31) / 32, ntask = nblk + rv.n_heavy_items;
-    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
-    for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; t < ntask; t += nw) {
-        if (t < nblk) {
-            const uint64_t u_l = t * 32 + lane;
-            uint32_t ns_l = 0;
-            if (u_l < n) {
-                const uint32_t d = rv.col[u_l + 1] - rv.col[u_l];
-                if (d > 0 && d <= AXBC_SPAN) ns_l = srcmask & ~seen[u_l];
+    uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
+    const uint64_t nhi = rv.n_heavy_items, nu = n_units(rv);
+    for (;;) {
+        const uint32_t t = grab_unit(ctr);
+        if (t >= nu) break;
+        if (t < nhi) {
+            const uint32_t u = rv.hitem_v[t];
+            const uint32_t ns = srcmask & ~seen[u];
+            if (!ns) continue;
+            const uint32_t b0 = rv.col[u] + rv.hitem_k[t] * AXBC_SPAN;
+            uint32_t acc;
+            const uint32_t nm =
+                pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg, acc);
+            if ((nm >> lane) & 1u) atomicAdd(&msigma[row_base(u) + lane], acc);
+            if (lane == 0 && nm) atomicOr(&fcur[u], nm);
+            continue;
+        }
+        const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
+        for (uint64_t lt = l0; lt < l0 + LIGHT_PER_UNIT && lt < rv.n_ltask; lt++) {
+            const uint32_t beg = rv.ltask[lt], cnt = rv.ltask[lt + 1] - beg;
+            uint32_t u_l = 0, ns_l = 0;
+            if (lane < cnt) {
+                u_l = rv.order[beg + lane];
+                if (rv.col[u_l + 1] > rv.col[u_l]) ns_l = srcmask & ~seen[u_l];
             }
             unsigned act = __ballot_sync(FULL_MASK, ns_l != 0);
             uint32_t mine = 0;
             while (act) {
                 const int j = __ffs(act) - 1;
                 act &= act - 1;
-                const uint32_t u = (uint32_t)(t * 32 + j);
+                const uint32_t u = __shfl_sync(FULL_MASK, u_l, j);
                 const uint32_t ns = __shfl_sync(FULL_MASK, ns_l, j);
                 uint32_t acc;
-                const uint32_t nm = pull_span(rv, ns, rv.col[u], rv.col[u + 1], fprev, msigma, acc);
+                const uint32_t nm =
+                    pull_span(rv, ns, rv.col[u], rv.col[u + 1], fprev, msigma, su, sg, acc);
                 if ((nm >> lane) & 1u) msigma[row_base(u) + lane] = acc;
                 if ((int)lane == j) mine = nm;
             }
             if (mine) fcur[u_l] = mine;
-        } else {
-            const uint64_t h = t - nblk;
-            const uint32_t u = rv.hitem_v[h];
-            const uint32_t ns = srcmask & ~seen[u];
-            if (!ns) continue;
-            const uint32_t b0 = rv.col[u] + rv.hitem_k[h] * AXBC_SPAN;
-            uint32_t acc;
-            const uint32_t nm =
-                pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, acc);
-            if ((nm >> lane) & 1u) atomicAdd(&msigma[row_base(u) + lane], acc);
-            if (lane == 0 && nm) atomicOr(&fcur[u], nm);
         }
     }
 }
@@ -261,16 +305,42 @@ __global__ void __launch_bounds__(BATCH_TPB) k_level_stats(uint64_t n, uint32_t 
     }
 }
 
+// Sum of the 8 staged successor terms of one group as a balanced tree (pairs
+// differing in the lowest position bit first).  mq_l points at lane l of row 0.
+__device__ __forceinline__ float tree8(const uint4 *su4, const uint4 *sg4, int g,
+                                       const float *__restrict__ mq_l, float sv, uint32_t lanebit)
+{
+    const uint4 ua = su4[2 * g], ub = su4[2 * g + 1];
+    const uint4 ga = sg4[2 * g], gb = sg4[2 * g + 1];
+    const uint32_t u[8] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w};
+    const uint32_t m[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
+    float t[8];
+#pragma unroll
+    for (int jj = 0; jj < 8; jj++) {
+        const bool h = (m[jj] & lanebit) != 0u;
+        const float q = h ? mq_l[(uint64_t)u[jj] * AXBC_W] : 0.0f;
+        t[jj] = h ? __fmul_rn(q, sv) : 0.0f;
+    }
+    const float a = __fadd_rn(__fadd_rn(t[0], t[1]), __fadd_rn(t[2], t[3]));
+    const float b = __fadd_rn(__fadd_rn(t[4], t[5]), __fadd_rn(t[6], t[7]));
+    return __fadd_rn(a, b);
+}
+
 // Canonical dependency sum of vertex v over adjacency positions [b0,b1) for
-// the pivots in f: lane s returns its span sum P_s.
-__device__ __forceinline__ float dep_span(const Adj &a, uint32_t v, uint32_t f, uint32_t b0,
+// the pivots in f.  q[u][s] = (delta_s[u] + 1) / sigma_s[u] was stored when
+// u's dependency was final, so a successor term is q * sigma_s[v], bit for bit
+// the reference's ((delta + 1) / sigma[r]) * sigma[c].  The 32 positions of a
+// chunk form four 8-position subtrees of the canonical tree; a subtree without
+// successors sums to +0 and is skipped.
+__device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, uint32_t b0,
                                           uint32_t b1, const uint32_t *__restrict__ fnext,
-                                          const uint32_t *__restrict__ msigma,
-                                          const float *__restrict__ mdelta, uint32_t *su,
-                                          uint32_t *sg)
+                                          const float *__restrict__ mq, uint32_t *su, uint32_t *sg)
 {
     const unsigned lane = lane_id();
-    const float sv = __uint2float_rn(((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u);
+    const uint32_t lanebit = 1u << lane;
+    const float *mq_l = mq + lane;
+    const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
+    const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
     float P = 0.0f;
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
@@ -279,30 +349,31 @@ __device__ __forceinline__ float dep_span(const Adj &a, uint32_t v, uint32_t f, 
             u = a.row[e];
             gm = fnext[u] & f;
         }
-        if (!__any_sync(FULL_MASK, gm != 0)) continue;
+        const unsigned pm = __ballot_sync(FULL_MASK, gm != 0);
+        if (!pm) continue;
         su[lane] = u;
         sg[lane] = gm;
         __syncwarp();
-        float t[32];
-#pragma unroll
-        for (int jj = 0; jj < 32; jj++) {
-            const uint32_t gj = sg[jj];
-            float x = 0.0f;
-            if ((gj >> lane) & 1u) {
-                const uint64_t o = row_base(su[jj]) + lane;
-                x = dep_term(mdelta[o], msigma[o], sv);
-            }
-            t[jj] = x;
-        }
-#pragma unroll
-        for (int w = 1; w < 32; w <<= 1) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 2 * w) t[j] = __fadd_rn(t[j], t[j + w]);
-        }
-        P = __fadd_rn(P, t[0]);
+        float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, g3 = 0.0f;
+        if (pm & 0x000000ffu) g0 = tree8(su4, sg4, 0, mq_l, sv, lanebit);
+        if (pm & 0x0000ff00u) g1 = tree8(su4, sg4, 1, mq_l, sv, lanebit);
+        if (pm & 0x00ff0000u) g2 = tree8(su4, sg4, 2, mq_l, sv, lanebit);
+        if (pm & 0xff000000u) g3 = tree8(su4, sg4, 3, mq_l, sv, lanebit);
+        P = __fadd_rn(P, __fadd_rn(__fadd_rn(g0, g1), __fadd_rn(g2, g3)));
         __syncwarp();
     }
     return P;
+}
+
+// delta and q of vertex v for the pivots in f
+__device__ __forceinline__ void write_dep(float *mdelta, float *mq, uint32_t v, uint32_t f,
+                                          float delta, uint32_t sig)
+{
+    const unsigned lane = lane_id();
+    if ((f >> lane) & 1u) {
+        mdelta[row_base(v) + lane] = delta;
+        mq[row_base(v) + lane] = __fdiv_rn(__fadd_rn(delta, 1.0f), __uint2float_rn(sig));
+    }
 }
 
 // Backward depth d for the pivots in dmask.  With no_succ (the deepest depth)
@@ -311,49 +382,58 @@ __global__ void __launch_bounds__(BATCH_TPB) k_bwd_m(Adj a, uint32_t dmask, int 
                                                      const uint32_t *__restrict__ fd,
                                                      const uint32_t *__restrict__ fnext,
                                                      const uint32_t *__restrict__ msigma,
-                                                     float *mdelta, float *mpartial,
-                                                     const uint32_t *__restrict__ reach)
+                                                     float *mdelta, float *mq, float *mpartial,
+                                                     const uint32_t *__restrict__ reach,
+                                                     uint32_t *ctr)
 {
-    __shared__ uint32_t s_u[BATCH_TPB], s_g[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
     const unsigned lane = lane_id();
     uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
-    const uint64_t n = a.n, nblk = (n + 31) / 32, ntask = nblk + a.n_heavy_items;
-    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
-    for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; t < ntask; t += nw) {
-        if (t < nblk) {
-            const uint64_t v_l = t * 32 + lane;
-            uint32_t f_l = 0;
-            if (v_l < n) {
+    const uint64_t nhi = a.n_heavy_items, nu = n_units(a);
+    for (;;) {
+        const uint32_t t = grab_unit(ctr);
+        if (t >= nu) break;
+        if (t < nhi) {
+            const uint32_t v = a.hitem_v[t];
+            const uint32_t f = fd[v] & dmask;
+            if (!f) continue;
+            float P = 0.0f;
+            if (!no_succ) {
+                const float sv = __uint2float_rn(((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u);
+                const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
+                P = dep_span(a, f, sv, b0, min(a.col[v + 1], b0 + AXBC_SPAN), fnext, mq, su, sg);
+            }
+            mpartial[(uint64_t)t * AXBC_W + lane] = P;
+            continue;
+        }
+        const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
+        for (uint64_t lt = l0; lt < l0 + LIGHT_PER_UNIT && lt < a.n_ltask; lt++) {
+            const uint32_t beg = a.ltask[lt], cnt = a.ltask[lt + 1] - beg;
+            uint32_t v_l = 0, f_l = 0;
+            if (lane < cnt) {
+                v_l = a.order[beg + lane];
                 f_l = fd[v_l] & dmask;
-                if (f_l && a.col[v_l + 1] - a.col[v_l] > AXBC_SPAN) f_l = 0;
             }
             unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
             while (act) {
                 const int j = __ffs(act) - 1;
                 act &= act - 1;
-                const uint32_t v = (uint32_t)(t * 32 + j);
+                const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
                 const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
+                const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
                 float P = 0.0f;
-                if (!no_succ) P = dep_span(a, v, f, a.col[v], a.col[v + 1], fnext, msigma, mdelta, su, sg);
-                if ((f >> lane) & 1u)
-                    mdelta[row_base(v) + lane] = __fadd_rn(__uint2float_rn(reach[v]), P);
+                if (!no_succ)
+                    P = dep_span(a, f, __uint2float_rn(sig), a.col[v], a.col[v + 1], fnext, mq, su, sg);
+                write_dep(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
             }
-        } else {
-            const uint64_t h = t - nblk;
-            const uint32_t v = a.hitem_v[h];
-            const uint32_t f = fd[v] & dmask;
-            if (!f) continue;
-            const uint32_t b0 = a.col[v] + a.hitem_k[h] * AXBC_SPAN;
-            float P = 0.0f;
-            if (!no_succ)
-                P = dep_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), fnext, msigma, mdelta, su, sg);
-            mpartial[h * AXBC_W + lane] = P;
         }
     }
 }
 
 __global__ void k_bwd_combine_m(Adj a, uint32_t dmask, const uint32_t *__restrict__ fd,
-                                float *mdelta, const float *__restrict__ mpartial,
+                                const uint32_t *__restrict__ msigma, float *mdelta, float *mq,
+                                const float *__restrict__ mpartial,
                                 const uint32_t *__restrict__ reach)
 {
     const unsigned lane = lane_id();
@@ -365,7 +445,8 @@ __global__ void k_bwd_combine_m(Adj a, uint32_t dmask, const uint32_t *__restric
         float acc = __uint2float_rn(reach[v]);
         for (uint32_t k = a.heavy_first[i]; k < a.heavy_first[i + 1]; k++)
             acc = __fadd_rn(acc, mpartial[(uint64_t)k * AXBC_W + lane]);
-        if ((f >> lane) & 1u) mdelta[row_base(v) + lane] = acc;
+        const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
+        write_dep(mdelta, mq, v, f, acc, sig);
     }
 }
 
@@ -380,6 +461,7 @@ __global__ void __launch_bounds__(BATCH_TPB) k_update_m(float *bc, const float *
     __shared__ uint32_t s_root[AXBC_W], s_reach[AXBC_W];
     __shared__ double s_p[AXBC_W];
     __shared__ unsigned long long s_nvt[AXBC_W];
+    __shared__ InvSplit s_iv[AXBC_W];
     const uint32_t napply = bi->napply;
     if (threadIdx.x < AXBC_W) {
         const int s = threadIdx.x;
@@ -391,11 +473,13 @@ __global__ void __launch_bounds__(BATCH_TPB) k_update_m(float *bc, const float *
             s_reach[s] = rv;
             s_p[s] = bi->p[s];
             s_nvt[s] = bi->nvis[s] + all;
+            s_iv[s] = inv_split(bi->p[s]);
         } else {
             s_root[s] = 0xffffffffu;
             s_reach[s] = 0;
             s_p[s] = 1.0;
             s_nvt[s] = 2;
+            s_iv[s] = inv_split(1.0);
         }
     }
     __syncthreads();
@@ -409,30 +493,26 @@ __global__ void __launch_bounds__(BATCH_TPB) k_update_m(float *bc, const float *
             // apply, and roots are reached
             continue;
         }
-        float d[AXBC_W];
         const float rf = __uint2float_rn(rv);
-        if (sv) {
-            const float4 *row = reinterpret_cast<const float4 *>(mdelta + row_base(v));
-#pragma unroll
-            for (int q = 0; q < AXBC_W / 4; q++) {
-                const float4 x = row[q];
-                d[4 * q] = x.x;
-                d[4 * q + 1] = x.y;
-                d[4 * q + 2] = x.z;
-                d[4 * q + 3] = x.w;
-            }
-        }
+        const float4 *row = reinterpret_cast<const float4 *>(mdelta + row_base(v));
         float b = bc[v];
+        for (int q = 0; q < AXBC_W / 4; q++) {
+            if (4 * q >= (int)napply) break;
+            float4 x = make_float4(rf, rf, rf, rf);
+            if ((sv >> (4 * q)) & 0xfu) x = row[q];
+            const float dq[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
-        for (int s = 0; s < AXBC_W; s++) {
-            if (s >= (int)napply) break;
-            if ((uint32_t)v == s_root[s]) {
-                if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
-                continue;
+            for (int k = 0; k < 4; k++) {
+                const int s = 4 * q + k;
+                if (s >= (int)napply) break;
+                if ((uint32_t)v == s_root[s]) {
+                    if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
+                    continue;
+                }
+                const float dv = ((sv >> s) & 1u) ? dq[k] : rf;
+                if (dv == 0.0f && s_p[s] > 0.0) continue;
+                b = __fadd_rn(b, bc_term_fast(dv, s_reach[s], s_p[s], s_iv[s]));
             }
-            const float dv = ((sv >> s) & 1u) ? d[s] : rf;
-            if (dv == 0.0f && s_p[s] > 0.0) continue;
-            b = __fadd_rn(b, bc_term(dv, s_reach[s], s_p[s]));
         }
         bc[v] = b;
     }
@@ -497,6 +577,8 @@ int axbc_ensure_batch(axbc_ctx *c)
     TRY(axbc_dalloc((void **)&c->seen, n * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->msigma, n * AXBC_W * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->mdelta, n * AXBC_W * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->mq, n * AXBC_W * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->task_ctr, 64, &c->bytes));
     TRY(axbc_dalloc((void **)&c->mpartial, (c->g->fwd.n_heavy_items + 1) * AXBC_W * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->bi, sizeof(BatchInfo), &c->bytes));
     CU(cudaMallocHost((void **)&c->bi_host, sizeof(BatchInfo)));
@@ -512,6 +594,15 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     const uint64_t n = g->n;
     cudaStream_t s = c->stream;
     const int grid = axbc_grid_for(c, BATCH_TPB, 8);
+    // dynamic kernels: as many blocks as stay resident; work comes from a counter
+    if (!c->dyn_blocks_per_sm) {
+        int a = 0, b = 0, d = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_m, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fwd_pull_m, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_bwd_m, BATCH_TPB, 0));
+        c->dyn_blocks_per_sm = std::max(1, std::min(a, std::min(b, d)));
+    }
+    const int dgrid = axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm);
     const size_t lvl_off = offsetof(BatchInfo, lvl_new);
     const size_t lvl_len = offsetof(BatchInfo, task_ctr) - lvl_off;
     const uint32_t srcmask = nsrc >= 32 ? FULL_MASK : ((1u << nsrc) - 1u);
@@ -547,9 +638,13 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         const bool push = (double)front * c->push_factor_batch < (double)unvis;
         {
             ProfScope ps(c, push ? KP_FWD_PUSH : KP_FWD_PULL, dte[L - 1] * (4.0 / W + 4.0));
-            if (push) k_fwd_push_m<<<grid, BATCH_TPB, 0, s>>>(g->fwd, fprev, fcur, c->seen, c->msigma);
-            else k_fwd_pull_m<<<grid, BATCH_TPB, 0, s>>>(g->rev, srcmask, fprev, fcur, c->seen,
-                                                        c->msigma);
+            CU(cudaMemsetAsync(c->task_ctr, 0, 4, s));
+            if (push)
+                k_fwd_push_m<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, fprev, fcur, c->seen, c->msigma,
+                                                        c->task_ctr);
+            else
+                k_fwd_pull_m<<<dgrid, BATCH_TPB, 0, s>>>(g->rev, srcmask, fprev, fcur, c->seen,
+                                                        c->msigma, c->task_ctr);
         }
         {
             ProfScope ps(c, KP_LEVEL_STATS, (double)n * 16.0);
@@ -593,13 +688,15 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         const double bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
         {
             ProfScope ps(c, KP_BWD, bytes);
-            k_bwd_m<<<grid, BATCH_TPB, 0, s>>>(g->fwd, dmask, d == Dmax, c->fmask[d], c->fmask[d + 1],
-                                               c->msigma, c->mdelta, c->mpartial, g->reach);
+            CU(cudaMemsetAsync(c->task_ctr, 0, 4, s));
+            k_bwd_m<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, dmask, d == Dmax, c->fmask[d],
+                                                c->fmask[d + 1], c->msigma, c->mdelta, c->mq,
+                                                c->mpartial, g->reach, c->task_ctr);
         }
         if (g->fwd.n_heavy) {
             ProfScope ps(c, KP_BWD_COMBINE, 0);
-            k_bwd_combine_m<<<(g->fwd.n_heavy + 7) / 8, 256, 0, s>>>(g->fwd, dmask, c->fmask[d],
-                                                                    c->mdelta, c->mpartial, g->reach);
+            k_bwd_combine_m<<<(g->fwd.n_heavy + 7) / 8, 256, 0, s>>>(
+                g->fwd, dmask, c->fmask[d], c->msigma, c->mdelta, c->mq, c->mpartial, g->reach);
         }
         CU_LAUNCH("backward level");
     }
@@ -697,5 +794,79 @@ extern "C" int axbc_get_batch_source(axbc_ctx *c, int src, uint32_t *sigma_host,
     axbc_dfree(sig);
     axbc_dfree(lvl);
     axbc_dfree(dl);
+    return AXBC_OK;
+}
+
+// ------------------------------------------------------------ self-test
+// The update's fast float(double(x)/p) against the double divide on n
+// generated (x, p) pairs: random magnitudes, random bit patterns, and x*p
+// products chosen to land next to float rounding midpoints.
+__device__ __forceinline__ uint64_t st_mix(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_selftest_div(uint64_t n, uint64_t seed, unsigned long long *bad,
+                               unsigned long long *slow)
+{
+    unsigned long long nb = 0, ns = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h1 = st_mix(seed ^ (i * 3 + 1)), h2 = st_mix(seed ^ (i * 3 + 2));
+        float x;
+        double p;
+        switch (i & 3) {
+        case 0:  // pivot probabilities: 1/N-like and products of small integers
+            x = (float)((h1 & 0xffffff) + 1) * ldexpf(1.0f, (int)((h1 >> 24) & 31) - 16);
+            p = 1.0 / (double)((h2 & 0xffffff) + 1);
+            break;
+        case 1:  // random float bits (positive, normal), random double p in (0,1]
+            x = __uint_as_float(((uint32_t)(h1 & 0x7fffffff) % 0x7f000000u) | 0x00800000u);
+            p = (double)((h2 >> 11) + 1) * 0x1.0p-53;
+            break;
+        case 2: {  // near midpoints: x/p = m + half ulp(m) +- tiny
+            const float m = (float)((h1 & 0xffffff) | 0x800000) * ldexpf(1.0f, (int)((h1 >> 24) & 15) - 8);
+            p = (double)((h2 >> 11) + 1) * 0x1.0p-53 + 1e-9;
+            const double target = ((double)m + (double)m * 0x1.0p-24) * (1.0 + ((int)(h2 & 7) - 3) * 0x1.0p-50);
+            x = (float)(target * p);
+            break;
+        }
+        default:  // integers times integers
+            x = (float)((h1 & 0xfffff) + 1);
+            p = (double)((h2 & 0xfff) + 1) / (double)((h2 >> 12 & 0xfffff) + 1);
+        }
+        if (!(x > 0.0f) || !(p > 0.0)) continue;
+        const InvSplit iv = inv_split(p);
+        const float f = div_to_float(x, p, iv);
+        const float e = __double2float_rn(__ddiv_rn((double)x, p));
+        if (__float_as_uint(f) != __float_as_uint(e)) nb++;
+        // count how often the exact path decided
+        const float a = __fmul_rn(x, iv.hi);
+        const float ee = __fmaf_rn(x, iv.hi, -a);
+        const float b = __fmaf_rn(x, iv.lo, ee);
+        const float s = __fadd_rn(a, b);
+        if (!iv.ok || __float_as_uint(s) != __float_as_uint(f)) ns++;
+    }
+    if (nb) atomicAdd(bad, nb);
+    if (ns) atomicAdd(slow, ns);
+}
+
+extern "C" int axbc_selftest_division(uint64_t n, uint64_t seed, uint64_t *mismatches,
+                                      uint64_t *exact_path)
+{
+    CHECK_ARG(mismatches, "axbc_selftest_division: null argument");
+    unsigned long long *d = nullptr;
+    TRY(axbc_dalloc((void **)&d, 16, nullptr));
+    CU(cudaMemset(d, 0, 16));
+    k_selftest_div<<<1024, 256>>>(n, seed, d, d + 1);
+    CU_LAUNCH("k_selftest_div");
+    unsigned long long h[2];
+    CU(cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost));
+    axbc_dfree(d);
+    *mismatches = h[0];
+    if (exact_path) *exact_path = h[1];
     return AXBC_OK;
 }

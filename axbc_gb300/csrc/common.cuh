@@ -68,6 +68,13 @@ struct Adj {
     uint32_t *heavy_first = nullptr;  // n_heavy first item index
     uint32_t *hitem_v = nullptr;      // n_heavy_items
     uint32_t *hitem_k = nullptr;      // span index of the item
+    // vertices by degree, descending (heavy ones first), and the light-vertex
+    // tasks: order[ltask[i] .. ltask[i+1]) holds at most 32 vertices whose
+    // degrees sum to about one span; dynamic kernels take heavy span items
+    // first, then these tasks, so the largest work is handed out first
+    uint32_t *order = nullptr;        // n
+    uint32_t *ltask = nullptr;        // n_ltask + 1 offsets into order
+    uint64_t n_ltask = 0;
     bool owns = true;
 };
 
@@ -176,6 +183,8 @@ struct axbc_ctx {
     std::vector<uint32_t *> fmask;  // one n-word mask array per level
     uint32_t *msigma = nullptr;     // n*32
     float *mdelta = nullptr;        // n*32
+    float *mq = nullptr;            // n*32: (delta + 1) / sigma, per pivot
+    uint32_t *task_ctr = nullptr;   // work counters of the dynamic kernels
     float *mpartial = nullptr;      // heavy items * 32
     BatchInfo *bi = nullptr;
     BatchInfo *bi_host = nullptr;  // pinned
@@ -209,6 +218,7 @@ struct axbc_ctx {
     double push_factor_batch = 1.0;
     uint64_t bytes = 0;
     int num_sms = 0;
+    int dyn_blocks_per_sm = 0;  // resident blocks of the dynamic kernels
 };
 
 // allocation with byte accounting
@@ -265,6 +275,52 @@ __device__ __forceinline__ float bc_term(float delta_v, uint32_t reach_v0, doubl
 {
     return __double2float_rn(__ddiv_rn((double)__fmul_rn(delta_v, __uint2float_rn(reach_v0 + 1u)), p));
 }
+// float(double(x) / p) for x >= 0 without the double divide in the common
+// case.  With 1/p split into float hi + lo (1/p computed once per pivot), x*hi
+// is formed exactly as a + e by Dekker's two-product (an FMA gives e), then
+// b = x*lo + e, so a + b approximates x/p to about 2^-46 relative.  s =
+// RN_float(a + b) equals the correctly rounded result unless x/p lies near the
+// midpoint between two floats; Knuth's TwoSum gives the exact residual of
+// s, and if it is within 2^-40 (relative) of half an ulp -- or s is a power of
+// two, tiny, huge or not finite -- the exact double divide decides.
+struct InvSplit {
+    float hi, lo;
+    int ok;  // 1: fast path usable for this p
+};
+__host__ __device__ __forceinline__ InvSplit inv_split(double p)
+{
+    InvSplit r{0.0f, 0.0f, 0};
+    if (!(p > 0.0) || p > 1e30 || p < 1e-30) return r;
+    const double inv = 1.0 / p;
+    r.hi = (float)inv;
+    r.lo = (float)(inv - (double)r.hi);
+    r.ok = 1;
+    return r;
+}
+__device__ __forceinline__ float div_to_float(float x, double p, InvSplit iv)
+{
+    if (iv.ok && x > 0.0f && x < 3.0e38f) {
+        const float a = __fmul_rn(x, iv.hi);
+        const float e = __fmaf_rn(x, iv.hi, -a);
+        const float b = __fmaf_rn(x, iv.lo, e);
+        const float s = __fadd_rn(a, b);
+        const float bb = __fsub_rn(s, a);
+        const float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+        const uint32_t bits = __float_as_uint(s);
+        const uint32_t ex = (bits >> 23) & 0xffu;
+        if (ex >= 40u && ex <= 210u && (bits & 0x7fffffu) != 0u) {
+            const float half_ulp = __uint_as_float((ex - 24u) << 23);
+            const float dist = fabsf(__fsub_rn(fabsf(err), half_ulp));
+            if (dist > __fmul_rn(s, 9.094947e-13f /* 2^-40 */)) return s;
+        }
+    }
+    return __double2float_rn(__ddiv_rn((double)x, p));
+}
+__device__ __forceinline__ float bc_term_fast(float delta_v, uint32_t reach_v0, double p, InvSplit iv)
+{
+    return div_to_float(__fmul_rn(delta_v, __uint2float_rn(reach_v0 + 1u)), p, iv);
+}
+
 // The root's increment (:277): reach_v0 * (nvisited - 2) converted to float.
 __device__ __forceinline__ float bc_root_term(uint32_t reach_v0, unsigned long long nvis_total)
 {

@@ -53,6 +53,40 @@ static void heavy_lists(const uint32_t *col, uint64_t n, std::vector<uint32_t> &
     if (maxdeg) *maxdeg = std::max(*maxdeg, md);
 }
 
+// Vertices by degree, descending (counting sort, ties by id), and light tasks
+// of at most 32 vertices and about one span of adjacency each.
+static void task_tables(const uint32_t *col, uint64_t n, std::vector<uint32_t> &order,
+                        std::vector<uint32_t> &ltask, uint64_t n_heavy)
+{
+    uint32_t md = 0;
+    for (uint64_t v = 0; v < n; v++) md = std::max(md, col[v + 1] - col[v]);
+    std::vector<uint64_t> cnt((size_t)md + 2, 0);
+    for (uint64_t v = 0; v < n; v++) cnt[md - (col[v + 1] - col[v])]++;
+    uint64_t acc = 0;
+    for (auto &c : cnt) {
+        uint64_t t = c;
+        c = acc;
+        acc += t;
+    }
+    order.resize(n);
+    for (uint64_t v = 0; v < n; v++) order[cnt[md - (col[v + 1] - col[v])]++] = (uint32_t)v;
+    // light tasks: weight = degree + 8 per vertex, budget one span
+    ltask.clear();
+    uint64_t i = n_heavy;
+    while (i < n) {
+        ltask.push_back((uint32_t)i);
+        uint64_t w = 0, k = 0;
+        while (i < n && k < 32) {
+            const uint64_t d = col[order[i] + 1] - col[order[i]];
+            if (k > 0 && w + d + 8 > AXBC_SPAN) break;
+            w += d + 8;
+            k++;
+            i++;
+        }
+    }
+    ltask.push_back((uint32_t)n);
+}
+
 static int upload_adj(Adj &a, const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
                       uint64_t *acct, uint32_t *maxdeg)
 {
@@ -77,6 +111,13 @@ static int upload_adj(Adj &a, const uint32_t *col, const uint32_t *row, uint64_t
         CU(cudaMemcpy(a.hitem_v, iv.data(), iv.size() * 4, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(a.hitem_k, ik.data(), ik.size() * 4, cudaMemcpyHostToDevice));
     }
+    std::vector<uint32_t> order, ltask;
+    task_tables(col, n, order, ltask, a.n_heavy);
+    a.n_ltask = ltask.size() - 1;
+    TRY(axbc_dalloc((void **)&a.order, n * 4, acct));
+    TRY(axbc_dalloc((void **)&a.ltask, ltask.size() * 4, acct));
+    CU(cudaMemcpy(a.order, order.data(), n * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(a.ltask, ltask.data(), ltask.size() * 4, cudaMemcpyHostToDevice));
     a.owns = true;
     return AXBC_OK;
 }
@@ -93,6 +134,8 @@ static void free_adj(Adj &a)
     axbc_dfree(a.heavy_first);
     axbc_dfree(a.hitem_v);
     axbc_dfree(a.hitem_k);
+    axbc_dfree(a.order);
+    axbc_dfree(a.ltask);
     a = Adj();
 }
 

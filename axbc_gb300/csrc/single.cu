@@ -263,6 +263,7 @@ __global__ void k_update1(float *bc, const float *__restrict__ delta, uint64_t n
     uint32_t all = 0;
     if (add_all) all = (add_sum ? (uint32_t)pc->reach_sum : 0u) + reach_v0;
     const unsigned long long nvt = nvt_base + all;
+    const InvSplit iv = inv_split(p);
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
          v += (uint64_t)gridDim.x * blockDim.x) {
         if (v == v0) {
@@ -271,7 +272,7 @@ __global__ void k_update1(float *bc, const float *__restrict__ delta, uint64_t n
         }
         const float dv = delta[v];
         if (dv == 0.0f && p > 0.0) continue;  // x + float(0/p) == x
-        bc[v] = __fadd_rn(bc[v], bc_term(dv, reach_v0, p));
+        bc[v] = __fadd_rn(bc[v], bc_term_fast(dv, reach_v0, p, iv));
     }
 }
 

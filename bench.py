@@ -188,6 +188,14 @@ def main():
                                W=args.width)
 
     seed = 4343543 + rank
+    # autotune the direction-switch factors on 32 trial pivots (set-up, untimed)
+    deg = G.deg()
+    rng = np.random.default_rng(1234)
+    trial = rng.choice(np.flatnonzero(deg > 0), size=32, replace=False).astype(np.uint32)
+    tuning = ctx.autotune(trial) if args.impl == "gb300" else None
+    if tuning:
+        config["tuning"] = {k: (round(v, 4) if isinstance(v, float) else v)
+                            for k, v in tuning.items() if "factor" in k or k == "batch_width"}
 
     if args.impl == "reference":
         if rank != 0:

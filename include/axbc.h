@@ -111,6 +111,20 @@ int axbc_ctx_bytes(const axbc_ctx *ctx, uint64_t *bytes);
  * pulls into unvisited vertices.  Defaults are built in. */
 int axbc_ctx_set_tuning(axbc_ctx *ctx, double push_factor_single, double push_factor_batch);
 
+/* Autotuner: times trial passes from the given pivots (the first 32 batched,
+ * the first 4 plain) over a grid of direction-switch factors and batch
+ * widths, keeps the fastest setting in the context and returns it.  bc is
+ * reset to zero afterwards. */
+typedef struct {
+    double push_factor_single;
+    double push_factor_batch;
+    int32_t batch_width;       /* fastest width <= 32 on these pivots */
+    int32_t pad;
+    double batch_te_per_s;     /* best trial rates */
+    double plain_te_per_s;
+} axbc_tuning;
+int axbc_autotune(axbc_ctx *ctx, const uint32_t *pivots, int npivots, int H, axbc_tuning *out);
+
 /* ---- per-pivot (plain form) ----
  * One Brandes pass from v0 with selection probability p: forward BFS with
  * uint32 path counts, backward float dependencies, bc update, exactly as
@@ -201,6 +215,13 @@ int axbc_ctx_profile(axbc_ctx *ctx, int enable);
 int axbc_ctx_profile_read(axbc_ctx *ctx, double *ms, uint64_t *count, double *bytes, int nkinds);
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
+
+/* ---- diagnostics ----
+ * The bc update computes float(double(x) / p) with a float two-product path
+ * and falls back to the double divide near float rounding midpoints; this
+ * runs both on n generated (x, p) pairs on the device and counts results
+ * that differ (must be 0) and how many took the double divide. */
+int axbc_selftest_division(uint64_t n, uint64_t seed, uint64_t *mismatches, uint64_t *exact_path);
 
 /* ---- static pivot distributions (device) ---- */
 /* (uint32)deg^2, neighbour-degree sums (sum_deg_neigh_func, src/axbc2d.c:

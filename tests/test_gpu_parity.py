@@ -302,3 +302,10 @@ def test_full_size_properties(axbc):
     for v, pp in zip(piv, p):
         ctx.run_pivot(v, pp, 0)
     assert_float_exact(ctx.bc(), bc_batch, "plain vs batched at scale 18")
+
+
+def test_division_fast_path_is_exact(axbc):
+    for seed in (1, 2, 3):
+        bad, slow = axbc.selftest_division(1 << 25, seed)
+        assert bad == 0
+        assert slow < (1 << 25) // 4  # the exact divide is the exception
