@@ -108,13 +108,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_for(kernel, workload):
-    """Per-launch DRAM bytes of `kernel` from a committed ncu summary, if any."""
+def traffic_for(kernel, graph_key):
+    """Per-launch DRAM bytes of `kernel` on this graph from the committed ncu summary
+    (profiles/traffic.json, written from profiles/dram_traffic_*.md), if any."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
-        ent = t.get(workload, {}).get(kernel)
+        ent = t.get(graph_key, {}).get(kernel)
         return None if ent is None else float(ent["dram_bytes_per_launch"])
     except Exception:
         return None
@@ -277,9 +278,14 @@ def main():
     ms, cnt, by = prof[kind]
     achieved = (by / (ms / 1000.0)) / 1e9 if ms > 0 else 0.0
     kernel = ax.PROF_KERNELS[kind]
-    traffic = traffic_for(kernel, workload)
+    traffic = traffic_for(kernel, f"kronecker-s{args.scale}-ef{args.edgefactor}")
+    avg_s = ms / max(cnt, 1) / 1000.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
+                "model": "survey 8d traversed-edge bytes: (4/W+8) B/TE backward, (4/W+4) "
+                         "forward; counts every edge of a reached vertex",
+                "dram_gbs_from_traffic": (traffic / avg_s / 1e9) if traffic else None,
+                "dram_frac_from_traffic": (traffic / avg_s / 1e9 / peak) if traffic else None,
                 "launches": cnt, "avg_launch_ms": ms / max(cnt, 1),
                 "algorithmic_bytes_per_launch": by / max(cnt, 1),
                 "peak_source": f"{peak_kind} hbm_gbs",
