@@ -121,11 +121,13 @@ def traffic_for(kernel, graph_key):
         return None
 
 
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+class _DeviceArray:
+    """A float32 device vector owned by the library, seen through
+    __cuda_array_interface__ (no copy)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (ptr, False),
+                                         "version": 3}
 
 
 def cpu_threads():
@@ -160,7 +162,8 @@ def oracle_sample(g_csc, pivots, probs, seconds, threads):
 
 def main():
     args = parse()
-    rank, world, local = dist_env()
+    from axbc_gb300 import sharding
+    rank, world, local = sharding.env()
     import numpy as np
 
     workload = (f"kronecker-s{args.scale}-ef{args.edgefactor} undirected, -z {args.z} "
@@ -188,7 +191,7 @@ def main():
         return ctx.run_sampled(z=args.z, nbfs=args.pivots, bader_c=0, nchecks=1, H=0, seed=seed,
                                W=args.width)
 
-    seed = 4343543 + rank
+    seed = sharding.rank_seed(4343543, rank)
     # autotune the direction-switch factors on 32 trial pivots (set-up, untimed)
     deg = G.deg()
     rng = np.random.default_rng(1234)
@@ -251,10 +254,12 @@ def main():
         last = step(seed)
         te += last["te"]
     if world > 1:
-        # the one exchange of the sharded path: sum the ranks' bc
+        # the one exchange of the sharded path: sum the ranks' bc (a device copy
+        # of the context's bc, reduced on the same stream)
         bc_t = torch.empty(G.n, dtype=torch.float32, device="cuda")
         with torch.cuda.stream(stream):
-            dist.all_reduce(bc_t)
+            bc_t.copy_(torch.as_tensor(_DeviceArray(ctx.bc_device_ptr(), G.n), device="cuda"))
+            sharding.sum_bc(bc_t)
     ev1.record(stream)
     torch.cuda.synchronize()
     launches = ctx.launches - l0
@@ -262,14 +267,8 @@ def main():
     ctx.profile(False)
     clk = clocks.stop()
     t = ev0.elapsed_time(ev1) / 1000.0
-    te_all = te
-    if world > 1:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-        tv = torch.tensor([te], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tv)
-        te_all = float(tv.item())
+    t = sharding.max_time(t, device="cuda")
+    te_all = sharding.total(float(te), device="cuda")
     value = te_all / t
 
     # roofline of the dominant kernel kind
