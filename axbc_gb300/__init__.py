@@ -96,6 +96,8 @@ _SIGS = {
     "axbc_ctx_profile_read": (C.c_int, [_P, _P, _P, _P, C.c_int]),
     "axbc_ctx_launches": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "axbc_autotune": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(Tuning)]),
+    "axbc_bc_pivot_static": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_uint64, C.c_uint32,
+                                       C.c_double, C.c_int, _P, _P, C.POINTER(PivotStats)]),
     "axbc_selftest_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_uint64)]),
 }

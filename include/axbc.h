@@ -142,6 +142,24 @@ typedef struct {
 
 int axbc_run_pivot(axbc_ctx *ctx, uint32_t v0, double p, int H, axbc_pivot_stats *stats);
 
+/* One plain Brandes pass from v0 that allocates no device memory.  It has
+ * no counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc: applications whose device memory belongs to another allocator or
+ * a fixed budget, loops that must not synchronise the device through
+ * cudaMalloc/cudaFree, or plug-ins that may only use the buffers handed to
+ * them.  col/row/reach (reach may be NULL: all zero) describe the graph in the
+ * reference's CSC layout and bc (n floats, updated in place) is the output --
+ * all device pointers owned by the caller; stream is a cudaStream_t or NULL.
+ * Scratch lives in one fixed __device__ array of about 5.6 MB that every GPU
+ * loading the library holds until exit; graphs above 2^18 vertices, or with
+ * more than 2^14 span items of vertices of degree > 1024, return
+ * AXBC_ERR_RANGE.  The first call on a device looks the array's address up
+ * (make it before any stream capture).  Calls share the array: overlapping
+ * calls race, so serialise them.  Results equal axbc_run_pivot's. */
+int axbc_bc_pivot_static(const uint32_t *col, const uint32_t *row, const uint32_t *reach,
+                         uint64_t n, uint64_t m, uint32_t v0, double p, int H, float *bc,
+                         void *stream, axbc_pivot_stats *stats);
+
 /* ---- batched (multi-source) form ----
  * k <= AXBC_MAX_BATCH pivots in one multi-source pass (one bit per pivot in a
  * 32-bit mask per vertex).  bc receives the pivots' updates in list order,
