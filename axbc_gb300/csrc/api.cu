@@ -68,7 +68,7 @@ void axbc_prof_start(axbc_ctx *c, int kind, double bytes)
 {
     c->launches++;
     if (!c->prof_on) return;
-    ProfRec r{kind, bytes, pool_get(c), pool_get(c)};
+    ProfRec r{kind, bytes, pool_get(c), pool_get(c), -1};
     if (r.a) cudaEventRecord(r.a, c->stream);
     c->prof.push_back(r);
 }
@@ -173,6 +173,17 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     axbc_dfree(c->mdelta);
     axbc_dfree(c->mq);
     axbc_dfree(c->task_ctr);
+    axbc_dfree(c->fmtab);
+    axbc_dfree(c->ctrs);
+    axbc_dfree(c->d_level_te);
+    axbc_dfree(c->d_level_cnt);
+    axbc_dfree(c->d_level_mode);
+    axbc_dfree(c->lpool);
+    axbc_dfree(c->lstart);
+    axbc_dfree(c->lcount);
+    axbc_dfree(c->lcap);
+    if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
+    if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
     axbc_dfree(c->mpartial);
     axbc_dfree(c->bi);
     if (c->bi_host) cudaFreeHost(c->bi_host);

@@ -16,10 +16,46 @@
 
 static __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * AXBC_W; }
 
+// Per-level vertex lists: the vertices whose level-L mask is nonzero, appended
+// by the forward kernels that set the mask.  A level whose list would exceed
+// its capacity keeps counting but stops storing (count > cap: no list), and
+// its consumers fall back to the degree-ordered task scan.
+struct LevelLists {
+    uint32_t *pool;
+    uint32_t *start;  // per level: offset into pool
+    uint32_t *count;  // per level: vertices appended
+    uint32_t *cap;    // per level: capacity
+};
+
+
+// Clear the level masks 2..lend of the previous batch (levels 0 and 1 are
+// cleared with memsets): a level whose list was stored has nonzero entries
+// only at its listed vertices; an overflowed level is cleared whole.
+__global__ void k_clean_levels(uint32_t *const *__restrict__ tab, const uint32_t *__restrict__ pool,
+                               const uint32_t *__restrict__ lstart,
+                               const uint32_t *__restrict__ lcount,
+                               const uint32_t *__restrict__ lcap, uint64_t n, int first)
+{
+    const int L = first + blockIdx.y;
+    uint32_t *f = tab[L];
+    const uint32_t cnt = lcount[L];
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
+    if (cnt <= lcap[L]) {
+        const uint32_t *lst = pool + lstart[L];
+        for (uint64_t i = tid; i < cnt; i += nt) f[lst[i]] = 0;
+    } else {
+        for (uint64_t i = tid; i < n; i += nt) f[i] = 0;
+    }
+}
+
 // roots: depth 0, sigma 1 (set_mlp_cuda, src/cuda_kernels.cu:862-876)
 __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, uint32_t *seen,
                              uint32_t *msigma, const uint32_t *__restrict__ col,
-                             const uint32_t *__restrict__ rcol, unsigned long long m)
+                             const uint32_t *__restrict__ rcol, unsigned long long m,
+                             double push_factor, unsigned long long *level_te,
+                             unsigned long long *level_cnt, LevelLists ll, uint32_t pool_cap,
+                             uint32_t list_max)
 {
     const int s = threadIdx.x;
     if (s == 0) {
@@ -28,6 +64,19 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, u
         bi->srcmask = nsrc >= 32 ? FULL_MASK : ((1u << nsrc) - 1u);
         bi->depth0mask = 0;
         bi->H = H;
+        bi->cur = 0;
+        bi->alive = 1;
+        bi->lend = 0;
+        bi->dmax = -1;
+        bi->bd = -1;
+        bi->push_factor = push_factor;
+        bi->lvl_te = 0;
+        bi->any_new = 0;
+        bi->pool_short = 0;
+    }
+    if (s < AXBC_W) {
+        bi->Ls[s] = 0;
+        bi->lvl_new[s] = 0;
     }
     unsigned long long fd = 0, rd = 0;
     if (s < nsrc) {
@@ -49,9 +98,22 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, u
         fd += __shfl_xor_sync(FULL_MASK, fd, o);
         rd += __shfl_xor_sync(FULL_MASK, rd, o);
     }
+    if (s < nsrc) ll.pool[s] = bi->root[s];
     if (s == 0) {
-        bi->front_deg = fd;
-        bi->unvis_deg = m - rd;
+        // a vertex counts as unvisited until every pivot has seen it: with one
+        // pivot its root is fully seen at once
+        const unsigned long long unvis = nsrc == 1 ? m - rd : m;
+        bi->front_deg = 0;
+        bi->unvis_deg = unvis;
+        bi->unvis_dec = 0;
+        bi->push_next = (double)fd * push_factor < (double)unvis;
+        level_te[0] = fd;
+        level_cnt[0] = nsrc;
+        ll.start[0] = 0;
+        ll.count[0] = nsrc;
+        ll.cap[0] = nsrc;
+        ll.start[1] = nsrc;
+        ll.cap[1] = min(list_max, pool_cap - nsrc);
     }
 }
 
@@ -74,12 +136,34 @@ __host__ __device__ __forceinline__ uint64_t n_units(const Adj &a)
     return a.n_heavy_items + (a.n_ltask + LIGHT_PER_UNIT - 1) / LIGHT_PER_UNIT;
 }
 
+__device__ __forceinline__ void list_append(const LevelLists &ll, int L, bool isnew, uint32_t v)
+{
+    const unsigned lane = lane_id();
+    const unsigned m = __ballot_sync(FULL_MASK, isnew);
+    if (!m) return;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&ll.count[L], (uint32_t)__popc(m));
+    base = __shfl_sync(FULL_MASK, base, leader);
+    const uint32_t idx = base + __popc(m & ((1u << lane) - 1u));
+    if (isnew && idx < ll.cap[L]) ll.pool[ll.start[L] + idx] = v;
+}
+
+// the stored list of level L, or nullptr when the level overflowed its capacity
+__device__ __forceinline__ const uint32_t *level_list(const LevelLists &ll, int L, uint32_t &cnt)
+{
+    cnt = ll.count[L];
+    if (cnt > ll.cap[L]) return nullptr;
+    return ll.pool + ll.start[L];
+}
+
 // Forward level L, push from the vertices of depth L-1: for each neighbour u
 // and each pivot s with v at depth L-1 and u unseen, sigma_s[u] += sigma_s[v]
 // and bit s joins u's level-L mask.  Atomics are fire-and-forget reductions.
 __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, uint32_t b0,
                                           uint32_t b1, const uint32_t *__restrict__ seen,
-                                          uint32_t *fcur, uint32_t *msigma)
+                                          uint32_t *fcur, uint32_t *msigma, const LevelLists &ll,
+                                          int L)
 {
     const unsigned lane = lane_id();
     const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
@@ -90,7 +174,8 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
             u = a.row[e];
             nm = f & ~seen[u];
         }
-        if (nm) atomicOr(&fcur[u], nm);
+        const uint32_t old = nm ? atomicOr(&fcur[u], nm) : 1u;
+        list_append(ll, L, old == 0u, u);
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
             const int j = __ffs(act) - 1;
@@ -102,13 +187,16 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
     }
 }
 
-__global__ void __launch_bounds__(BATCH_TPB) k_fwd_push_m(Adj a, const uint32_t *__restrict__ fprev,
-                                                          uint32_t *fcur,
-                                                          const uint32_t *__restrict__ seen,
-                                                          uint32_t *msigma, uint32_t *ctr)
+__device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__restrict__ fprev,
+                                              uint32_t *fcur, const uint32_t *__restrict__ seen,
+                                              uint32_t *msigma, uint32_t *ctr, const LevelLists &ll,
+                                              int L)
 {
     const unsigned lane = lane_id();
-    const uint64_t nhi = a.n_heavy_items, nu = n_units(a);
+    const uint64_t nhi = a.n_heavy_items;
+    uint32_t lcnt = 0;
+    const uint32_t *lst = level_list(ll, L - 1, lcnt);  // the frontier, when stored
+    const uint64_t nu = lst ? nhi + (lcnt + 31) / 32 : n_units(a);
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -117,7 +205,24 @@ __global__ void __launch_bounds__(BATCH_TPB) k_fwd_push_m(Adj a, const uint32_t 
             const uint32_t f = fprev[v];
             if (!f) continue;
             const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
-            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma);
+            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma, ll, L);
+            continue;
+        }
+        if (lst) {
+            const uint32_t i = (uint32_t)(t - nhi) * 32 + lane;
+            uint32_t v_l = 0, f_l = 0;
+            if (i < lcnt) {
+                v_l = lst[i];
+                if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fprev[v_l];
+            }
+            unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
+            while (act) {
+                const int j = __ffs(act) - 1;
+                act &= act - 1;
+                const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
+                const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
+                push_span(a, v, f, a.col[v], a.col[v + 1], seen, fcur, msigma, ll, L);
+            }
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
@@ -134,7 +239,7 @@ __global__ void __launch_bounds__(BATCH_TPB) k_fwd_push_m(Adj a, const uint32_t 
                 act &= act - 1;
                 const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
                 const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
-                push_span(a, v, f, a.col[v], a.col[v + 1], seen, fcur, msigma);
+                push_span(a, v, f, a.col[v], a.col[v + 1], seen, fcur, msigma, ll, L);
             }
         }
     }
@@ -186,15 +291,13 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
     return __ballot_sync(FULL_MASK, found);
 }
 
-__global__ void __launch_bounds__(BATCH_TPB) k_fwd_pull_m(Adj rv, uint32_t srcmask,
-                                                          const uint32_t *__restrict__ fprev,
-                                                          uint32_t *fcur,
-                                                          const uint32_t *__restrict__ seen,
-                                                          uint32_t *msigma, uint32_t *ctr)
+__device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
+                                              const uint32_t *__restrict__ fprev, uint32_t *fcur,
+                                              const uint32_t *__restrict__ seen, uint32_t *msigma,
+                                              uint32_t *ctr, uint32_t *su, uint32_t *sg,
+                                              const LevelLists &ll, int L)
 {
-    __shared__ uint32_t s_u[BATCH_TPB], s_g[BATCH_TPB];
     const unsigned lane = lane_id();
-    uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
     const uint64_t nhi = rv.n_heavy_items, nu = n_units(rv);
     for (;;) {
         const uint32_t t = grab_unit(ctr);
@@ -208,7 +311,9 @@ __global__ void __launch_bounds__(BATCH_TPB) k_fwd_pull_m(Adj rv, uint32_t srcma
             const uint32_t nm =
                 pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg, acc);
             if ((nm >> lane) & 1u) atomicAdd(&msigma[row_base(u) + lane], acc);
-            if (lane == 0 && nm) atomicOr(&fcur[u], nm);
+            bool first = false;
+            if (lane == 0 && nm) first = atomicOr(&fcur[u], nm) == 0u;
+            list_append(ll, L, first, u);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
@@ -233,40 +338,80 @@ __global__ void __launch_bounds__(BATCH_TPB) k_fwd_pull_m(Adj rv, uint32_t srcma
                 if ((int)lane == j) mine = nm;
             }
             if (mine) fcur[u_l] = mine;
+            list_append(ll, L, mine != 0u, u_l);
         }
     }
 }
 
-// After level L: fold the level mask into `seen` and count, per pivot, the
-// vertices reached, their degree sum and their reach sum.
-__global__ void __launch_bounds__(BATCH_TPB) k_level_stats(uint64_t n, uint32_t srcmask,
-                                                           const uint32_t *__restrict__ fcur,
-                                                           uint32_t *seen,
-                                                           const uint32_t *__restrict__ col,
-                                                           const uint32_t *__restrict__ rcol,
-                                                           const uint32_t *__restrict__ reach,
-                                                           BatchInfo *bi)
+// One forward level, device-driven: the level is bi->cur + 1 and the direction
+// bi->push_next (set by the previous k_level_advance); a no-op once a level
+// discovered nothing.
+__global__ void __launch_bounds__(BATCH_TPB, 8) k_fwd_step(Adj a, Adj rv, const BatchInfo *__restrict__ bi,
+                                                        uint32_t *const *__restrict__ tab,
+                                                        const uint32_t *__restrict__ seen,
+                                                        uint32_t *msigma, uint32_t *ctrs,
+                                                        LevelLists ll)
 {
+    __shared__ uint32_t s_u[BATCH_TPB], s_g[BATCH_TPB];
+    if (!bi->alive) return;
+    const int L = bi->cur + 1;
+    uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
+    if (bi->push_next) fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L);
+    else fwd_pull_body(rv, bi->srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, su, sg, ll, L);
+}
+
+// After level L = bi->cur + 1: fold the level mask into `seen` and count, per
+// pivot, the vertices reached, their degree sum and their reach sum; subtract
+// from the unvisited-edge total the in-degrees of vertices now seen by every
+// pivot.  Visits only level L's list when stored.
+__device__ __forceinline__ void stats_vertex(uint64_t u, uint32_t srcmask,
+                                             const uint32_t *__restrict__ fcur, uint32_t *seen,
+                                             const uint32_t *__restrict__ col,
+                                             const uint32_t *__restrict__ rcol,
+                                             const uint32_t *__restrict__ reach, uint32_t &nm,
+                                             uint32_t &d, uint32_t &r, unsigned long long &fdeg,
+                                             unsigned long long &udec, bool &any)
+{
+    nm = fcur[u];
+    if (!nm) return;
+    any = true;
+    const uint32_t sn = seen[u];
+    const uint32_t sn2 = sn | nm;
+    seen[u] = sn2;
+    d = col[u + 1] - col[u];
+    r = reach[u];
+    fdeg += d;
+    if ((sn & srcmask) != srcmask && (sn2 & srcmask) == srcmask) udec += rcol[u + 1] - rcol[u];
+}
+
+__global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo *bi,
+                                                          uint32_t *const *__restrict__ tab,
+                                                          uint32_t *seen,
+                                                          const uint32_t *__restrict__ col,
+                                                          const uint32_t *__restrict__ rcol,
+                                                          const uint32_t *__restrict__ reach,
+                                                          LevelLists ll)
+{
+    if (!bi->alive) return;
+    const int L = bi->cur + 1;
+    const uint32_t srcmask = bi->srcmask;
+    const uint32_t *__restrict__ fcur = tab[L];
     const unsigned lane = lane_id();
-    const uint64_t nblk = (n + 31) / 32;
-    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
-    unsigned long long cnt = 0, te = 0, rs = 0, fdeg = 0, udeg = 0;
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t lcnt = 0;
+    const uint32_t *lst = level_list(ll, L, lcnt);
+    const uint64_t items = lst ? lcnt : n;
+    const uint64_t nblk = (items + 31) / 32;
+    const uint64_t nw = nthreads / 32;
+    unsigned long long cnt = 0, te = 0, rs = 0, fdeg = 0, udec = 0;
     bool any = false;
-    for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; t < nblk; t += nw) {
-        const uint64_t u = t * 32 + lane;
+    for (uint64_t t = tid / 32; t < nblk; t += nw) {
+        const uint64_t i = t * 32 + lane;
         uint32_t nm = 0, d = 0, r = 0;
-        if (u < n) {
-            nm = fcur[u];
-            uint32_t sn = seen[u];
-            if (nm) {
-                any = true;
-                sn |= nm;
-                seen[u] = sn;
-                d = col[u + 1] - col[u];
-                r = reach[u];
-                fdeg += d;
-            }
-            if (srcmask & ~sn) udeg += rcol[u + 1] - rcol[u];
+        if (i < items) {
+            const uint64_t u = lst ? lst[i] : i;
+            stats_vertex(u, srcmask, fcur, seen, col, rcol, reach, nm, d, r, fdeg, udec, any);
         }
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
@@ -295,14 +440,60 @@ __global__ void __launch_bounds__(BATCH_TPB) k_level_stats(uint64_t n, uint32_t 
     }
     for (int o = 16; o; o >>= 1) {
         fdeg += __shfl_xor_sync(FULL_MASK, fdeg, o);
-        udeg += __shfl_xor_sync(FULL_MASK, udeg, o);
+        udec += __shfl_xor_sync(FULL_MASK, udec, o);
     }
     any = __any_sync(FULL_MASK, any);
     if (lane == 0) {
         if (fdeg) atomicAdd(&bi->front_deg, fdeg);
-        if (udeg) atomicAdd(&bi->unvis_deg, udeg);
+        if (udec) atomicAdd(&bi->unvis_dec, udec);
         if (any) atomicOr(&bi->any_new, 1u);
     }
+}
+
+// Close forward level L = bi->cur + 1: per-pivot termination, the per-level
+// totals, the direction of the next level, and -- once nothing was discovered
+// -- the deepest depth and the depth-0 pivots of the backward pass.
+__global__ void k_level_advance(BatchInfo *bi, unsigned long long *level_te,
+                                unsigned long long *level_cnt, int32_t *level_mode,
+                                LevelLists ll, uint32_t pool_cap, uint32_t list_max)
+{
+    const unsigned s = threadIdx.x;
+    if (!bi->alive) return;
+    const int L = bi->cur + 1;
+    const uint32_t nsrc = bi->nsrc;
+    const unsigned long long nw = s < nsrc ? bi->lvl_new[s] : 0ull;
+    if (s < nsrc && bi->Ls[s] == 0 && nw == 0) bi->Ls[s] = L;
+    unsigned long long cnt = nw;
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
+    const bool two = s < nsrc && bi->Ls[s] == 2;
+    const uint32_t d0 = __ballot_sync(FULL_MASK, two);
+    __syncwarp();
+    if (s == 0) {
+        level_te[L] = bi->lvl_te;
+        level_cnt[L] = cnt;
+        level_mode[L] = bi->push_next;
+        bi->unvis_deg -= bi->unvis_dec;
+        bi->unvis_dec = 0;
+        const bool push = (double)bi->front_deg * bi->push_factor < (double)bi->unvis_deg;
+        // where level L+1's list goes and how long it may grow
+        const uint32_t used = ll.start[L] + (ll.count[L] <= ll.cap[L] ? ll.count[L] : 0u);
+        ll.start[L + 1] = used;
+        ll.cap[L + 1] = min(list_max, pool_cap - min(pool_cap, used));
+        if (pool_cap - min(pool_cap, used) < list_max) bi->pool_short = 1;
+        if (!bi->any_new) {
+            bi->alive = 0;
+            bi->lend = L;
+            bi->dmax = L - 1;
+            bi->bd = L - 1;
+            bi->depth0mask = d0;
+        }
+        bi->push_next = push;
+        bi->cur = L;
+        bi->lvl_te = 0;
+        bi->front_deg = 0;
+        bi->any_new = 0;
+    }
+    if (s < AXBC_W) bi->lvl_new[s] = 0;
 }
 
 // Sum of the 8 staged successor terms of one group as a balanced tree (pairs
@@ -378,19 +569,39 @@ __device__ __forceinline__ void write_dep(float *mdelta, float *mq, uint32_t v, 
 
 // Backward depth d for the pivots in dmask.  With no_succ (the deepest depth)
 // nothing lies below, so delta = reach.
-__global__ void __launch_bounds__(BATCH_TPB) k_bwd_m(Adj a, uint32_t dmask, int no_succ,
-                                                     const uint32_t *__restrict__ fd,
-                                                     const uint32_t *__restrict__ fnext,
-                                                     const uint32_t *__restrict__ msigma,
-                                                     float *mdelta, float *mq, float *mpartial,
-                                                     const uint32_t *__restrict__ reach,
-                                                     uint32_t *ctr)
+__device__ __forceinline__ void bwd_vertices(const Adj &a, uint32_t v_l, uint32_t f_l, int no_succ,
+                                             const uint32_t *__restrict__ fnext,
+                                             const uint32_t *__restrict__ msigma, float *mdelta,
+                                             float *mq, const uint32_t *__restrict__ reach,
+                                             uint32_t *su, uint32_t *sg)
 {
-    __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
-    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
     const unsigned lane = lane_id();
-    uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
-    const uint64_t nhi = a.n_heavy_items, nu = n_units(a);
+    unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
+    while (act) {
+        const int j = __ffs(act) - 1;
+        act &= act - 1;
+        const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
+        const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
+        const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
+        float P = 0.0f;
+        if (!no_succ)
+            P = dep_span(a, f, __uint2float_rn(sig), a.col[v], a.col[v + 1], fnext, mq, su, sg);
+        write_dep(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
+    }
+}
+
+__device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_succ,
+                                         const uint32_t *__restrict__ fd,
+                                         const uint32_t *__restrict__ fnext,
+                                         const uint32_t *__restrict__ msigma, float *mdelta,
+                                         float *mq, float *mpartial,
+                                         const uint32_t *__restrict__ reach, uint32_t *ctr,
+                                         uint32_t *su, uint32_t *sg, const uint32_t *lst,
+                                         uint32_t lcnt)
+{
+    const unsigned lane = lane_id();
+    const uint64_t nhi = a.n_heavy_items;
+    const uint64_t nu = lst ? nhi + (lcnt + 31) / 32 : n_units(a);
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -407,6 +618,16 @@ __global__ void __launch_bounds__(BATCH_TPB) k_bwd_m(Adj a, uint32_t dmask, int 
             mpartial[(uint64_t)t * AXBC_W + lane] = P;
             continue;
         }
+        if (lst) {
+            const uint32_t i = (uint32_t)(t - nhi) * 32 + lane;
+            uint32_t v_l = 0, f_l = 0;
+            if (i < lcnt) {
+                v_l = lst[i];
+                if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fd[v_l] & dmask;
+            }
+            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg);
+            continue;
+        }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
         for (uint64_t lt = l0; lt < l0 + LIGHT_PER_UNIT && lt < a.n_ltask; lt++) {
             const uint32_t beg = a.ltask[lt], cnt = a.ltask[lt + 1] - beg;
@@ -415,26 +636,37 @@ __global__ void __launch_bounds__(BATCH_TPB) k_bwd_m(Adj a, uint32_t dmask, int 
                 v_l = a.order[beg + lane];
                 f_l = fd[v_l] & dmask;
             }
-            unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
-            while (act) {
-                const int j = __ffs(act) - 1;
-                act &= act - 1;
-                const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
-                const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
-                const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
-                float P = 0.0f;
-                if (!no_succ)
-                    P = dep_span(a, f, __uint2float_rn(sig), a.col[v], a.col[v + 1], fnext, mq, su, sg);
-                write_dep(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
-            }
+            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg);
         }
     }
 }
 
-__global__ void k_bwd_combine_m(Adj a, uint32_t dmask, const uint32_t *__restrict__ fd,
-                                const uint32_t *__restrict__ msigma, float *mdelta, float *mq,
-                                const float *__restrict__ mpartial,
-                                const uint32_t *__restrict__ reach)
+// One backward depth, device-driven: d = bi->bd (a no-op once below 0).
+__global__ void __launch_bounds__(BATCH_TPB, 8) k_bwd_step(Adj a, const BatchInfo *__restrict__ bi,
+                                                        uint32_t *const *__restrict__ tab,
+                                                        const uint32_t *__restrict__ msigma,
+                                                        float *mdelta, float *mq, float *mpartial,
+                                                        const uint32_t *__restrict__ reach,
+                                                        uint32_t *ctrs, LevelLists ll)
+{
+    __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
+    const int d = bi->bd;
+    if (d < 0) return;
+    const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
+    if (!dmask) return;
+    uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
+    uint32_t lcnt = 0;
+    const uint32_t *lst = level_list(ll, d, lcnt);
+    bwd_body(a, dmask, d == bi->dmax, tab[d], tab[d + 1], msigma, mdelta, mq, mpartial, reach,
+             ctrs + 2 * d + 1, su, sg, lst, lcnt);
+}
+
+__device__ __forceinline__ void combine_body(const Adj &a, uint32_t dmask,
+                                             const uint32_t *__restrict__ fd,
+                                             const uint32_t *__restrict__ msigma, float *mdelta,
+                                             float *mq, const float *__restrict__ mpartial,
+                                             const uint32_t *__restrict__ reach)
 {
     const unsigned lane = lane_id();
     const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
@@ -448,6 +680,24 @@ __global__ void k_bwd_combine_m(Adj a, uint32_t dmask, const uint32_t *__restric
         const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
         write_dep(mdelta, mq, v, f, acc, sig);
     }
+}
+
+__global__ void k_bwd_combine_step(Adj a, const BatchInfo *__restrict__ bi,
+                                   uint32_t *const *__restrict__ tab,
+                                   const uint32_t *__restrict__ msigma, float *mdelta, float *mq,
+                                   const float *__restrict__ mpartial,
+                                   const uint32_t *__restrict__ reach)
+{
+    const int d = bi->bd;
+    if (d < 0) return;
+    const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
+    if (!dmask) return;
+    combine_body(a, dmask, tab[d], msigma, mdelta, mq, mpartial, reach);
+}
+
+__global__ void k_bwd_advance(BatchInfo *bi)
+{
+    if (bi->bd >= 0) bi->bd--;
 }
 
 // bc update for pivots 0..napply-1 in order (update_bc, src/cuda_kernels.cu:
@@ -560,13 +810,52 @@ __global__ void k_source_view(int s, int levels, uint32_t *const *fm, const uint
     }
 }
 
+static int ensure_level_tables(axbc_ctx *c)
+{
+    if (c->fmtab) return AXBC_OK;
+    TRY(axbc_dalloc((void **)&c->fmtab, AXBC_MAX_LEVELS * sizeof(uint32_t *), &c->bytes));
+    TRY(axbc_dalloc((void **)&c->ctrs, 2 * AXBC_MAX_LEVELS * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->d_level_te, AXBC_MAX_LEVELS * 8, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->d_level_cnt, AXBC_MAX_LEVELS * 8, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->d_level_mode, AXBC_MAX_LEVELS * 4, &c->bytes));
+    // level lists: room for every vertex about twice over; a level may hold
+    // up to n/8 vertices before it falls back to the task scan
+    c->lpool_cap = (uint32_t)std::min<uint64_t>(2 * c->g->n + 64, 0xffffffffull);
+    TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)c->lpool_cap * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->lstart, AXBC_MAX_LEVELS * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->lcount, AXBC_MAX_LEVELS * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->lcap, AXBC_MAX_LEVELS * 4, &c->bytes));
+    return AXBC_OK;
+}
+
+static LevelLists lists_of(const axbc_ctx *c)
+{
+    return LevelLists{c->lpool, c->lstart, c->lcount, c->lcap};
+}
+
+static uint32_t list_max_of(const axbc_ctx *c)
+{
+    return (uint32_t)std::max<uint64_t>(64, c->g->n / 8);
+}
+
+// Level masks 0..levels-1 exist, and their pointers are in the device table.
 int axbc_batch_levels_alloc(axbc_ctx *c, int levels)
 {
+    TRY(ensure_level_tables(c));
+    if (levels > AXBC_MAX_LEVELS) {
+        axbc_set_error("traversal deeper than %d levels", AXBC_MAX_LEVELS - 2);
+        return AXBC_ERR_RANGE;
+    }
+    const size_t have = c->fmask.size();
     while ((int)c->fmask.size() < levels) {
         uint32_t *p = nullptr;
         TRY(axbc_dalloc((void **)&p, c->g->n * 4, &c->bytes));
+        CU(cudaMemset(p, 0, c->g->n * 4));
         c->fmask.push_back(p);
     }
+    if (c->fmask.size() > have)
+        CU(cudaMemcpy(c->fmtab + have, c->fmask.data() + have,
+                      (c->fmask.size() - have) * sizeof(uint32_t *), cudaMemcpyHostToDevice));
     return AXBC_OK;
 }
 
@@ -583,126 +872,229 @@ int axbc_ensure_batch(axbc_ctx *c)
     TRY(axbc_dalloc((void **)&c->bi, sizeof(BatchInfo), &c->bytes));
     CU(cudaMallocHost((void **)&c->bi_host, sizeof(BatchInfo)));
     CU(cudaMemset(c->bi, 0, sizeof(BatchInfo)));
-    TRY(axbc_batch_levels_alloc(c, 8));
+    TRY(axbc_batch_levels_alloc(c, 10));
     return AXBC_OK;
 }
 
-// Forward and backward passes of the batch whose roots/p are in c->bi.
+static int dyn_grid(axbc_ctx *c)
+{
+    // dynamic kernels: as many blocks as stay resident; work comes from counters
+    if (!c->dyn_blocks_per_sm) {
+        int a = 0, b = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_step, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step, BATCH_TPB, 0));
+        c->dyn_blocks_per_sm = std::max(1, std::min(a, b));
+    }
+    return axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm);
+}
+
+// the kernels of one forward level / one backward depth, in stream order
+static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
+{
+    axbc_graph *g = c->g;
+    const LevelLists ll = lists_of(c);
+    k_fwd_step<<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, g->rev, c->bi, c->fmtab, c->seen, c->msigma,
+                                                   c->ctrs, ll);
+    k_stats_step<<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->fwd.col,
+                                                     g->rev.col, g->reach, ll);
+    k_level_advance<<<1, 32, 0, c->stream>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode,
+                                             ll, c->lpool_cap, list_max_of(c));
+}
+
+static void bwd_step_kernels(axbc_ctx *c, int dgrid)
+{
+    axbc_graph *g = c->g;
+    k_bwd_step<<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
+                                                   c->mq, c->mpartial, g->reach, c->ctrs,
+                                                   lists_of(c));
+    if (g->fwd.n_heavy)
+        k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, c->stream>>>(
+            g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach);
+    k_bwd_advance<<<1, 1, 0, c->stream>>>(c->bi);
+}
+
+// Capture one forward step and one backward step as CUDA graphs; every
+// argument is fixed for the context (levels come from device state).
+static int capture_steps(axbc_ctx *c, int dgrid, int sgrid)
+{
+    if (c->fwd_step_exec && c->bwd_step_exec) return AXBC_OK;
+    for (int which = 0; which < 2; which++) {
+        cudaGraph_t gr = nullptr;
+        CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        if (which == 0) fwd_step_kernels(c, dgrid, sgrid);
+        else bwd_step_kernels(c, dgrid);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+        if (e != cudaSuccess) return axbc_cuda_fail(e, "capture level step", __FILE__, __LINE__);
+        e = cudaGraphInstantiate(which == 0 ? &c->fwd_step_exec : &c->bwd_step_exec, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return axbc_cuda_fail(e, "instantiate level step", __FILE__, __LINE__);
+    }
+    return AXBC_OK;
+}
+
+// Forward and backward passes of the batch whose roots/p are in c->bi.  The
+// host launches forward level steps in blocks (8, then doubling) and reads
+// the level state once per block; steps past the last level do nothing.
 int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
 {
     axbc_graph *g = c->g;
     const uint64_t n = g->n;
     cudaStream_t s = c->stream;
-    const int grid = axbc_grid_for(c, BATCH_TPB, 8);
-    // dynamic kernels: as many blocks as stay resident; work comes from a counter
-    if (!c->dyn_blocks_per_sm) {
-        int a = 0, b = 0, d = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_m, BATCH_TPB, 0));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fwd_pull_m, BATCH_TPB, 0));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_bwd_m, BATCH_TPB, 0));
-        c->dyn_blocks_per_sm = std::max(1, std::min(a, std::min(b, d)));
-    }
-    const int dgrid = axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm);
-    const size_t lvl_off = offsetof(BatchInfo, lvl_new);
-    const size_t lvl_len = offsetof(BatchInfo, task_ctr) - lvl_off;
-    const uint32_t srcmask = nsrc >= 32 ? FULL_MASK : ((1u << nsrc) - 1u);
+    const int sgrid = axbc_grid_for(c, BATCH_TPB, 8);
+    const int dgrid = dyn_grid(c);
+    const bool prof = c->prof_on;
+    TRY(ensure_level_tables(c));
+    TRY(axbc_batch_levels_alloc(c, 10));
+    if (!prof) TRY(capture_steps(c, dgrid, sgrid));
 
+    // the previous batch's level masks back to zero, then a larger list pool
+    // if that batch ran out of list space
+    if (c->prev_lend >= 2) {
+        dim3 cg(axbc_grid_for(c, 256, 2), c->prev_lend - 1);
+        k_clean_levels<<<cg, 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount, c->lcap, n, 2);
+        CU_LAUNCH("k_clean_levels");
+        c->launches++;
+    }
+    c->prev_lend = 0;
+    if (c->pool_short && c->lpool_cap < 32 * n + 64) {
+        CU(cudaStreamSynchronize(s));
+        axbc_dfree(c->lpool);
+        c->lpool = nullptr;
+        c->lpool_cap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, 32 * n + 64),
+                                                    0xffffffffull);
+        TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)c->lpool_cap * 4, &c->bytes));
+        c->pool_short = false;
+        if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
+        if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
+        c->fwd_step_exec = c->bwd_step_exec = nullptr;
+        if (!prof) TRY(capture_steps(c, dgrid, sgrid));
+    }
     CU(cudaMemsetAsync(c->seen, 0, n * 4, s));
     CU(cudaMemsetAsync(c->fmask[0], 0, n * 4, s));
+    CU(cudaMemsetAsync(c->fmask[1], 0, n * 4, s));
     CU(cudaMemsetAsync(c->msigma, 0, n * AXBC_W * 4, s));
+    CU(cudaMemsetAsync(c->ctrs, 0, 2 * AXBC_MAX_LEVELS * 4, s));
+    CU(cudaMemsetAsync(c->lcount, 0, AXBC_MAX_LEVELS * 4, s));
+    const LevelLists ll = lists_of(c);
+    const uint32_t lmax = list_max_of(c);
     {
         ProfScope ps(c, KP_LEVEL_STATS, 0);
         k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->fmask[0], c->seen, c->msigma, g->fwd.col,
-                                      g->rev.col, g->m);
+                                      g->rev.col, g->m, c->push_factor_batch, c->d_level_te,
+                                      c->d_level_cnt, ll, c->lpool_cap, lmax);
     }
     CU_LAUNCH("k_batch_init");
-    CU(cudaMemcpyAsync((char *)c->bi_host + lvl_off, (char *)c->bi + lvl_off, lvl_len,
-                       cudaMemcpyDeviceToHost, s));
-    CU(cudaStreamSynchronize(s));
-    uint64_t front = c->bi_host->front_deg, unvis = c->bi_host->unvis_deg;
-    // per depth: degree sum over (vertex, pivot) pairs and pair count, for
-    // the traversed-edge byte model of the profiling hooks
-    std::vector<double> dte(1, (double)front), dcnt(1, (double)nsrc);
-    const double W = nsrc;
 
-    int Ls[AXBC_W];
-    for (int i = 0; i < AXBC_W; i++) Ls[i] = 0;
-    uint32_t alive = srcmask;
-    int L = 0;
+    const size_t ctl_off = offsetof(BatchInfo, cur);
+    const size_t ctl_len = offsetof(BatchInfo, push_factor) - ctl_off;
+    const size_t prof_first = c->prof.size();
+    int launched = 0, K = 8;
     for (;;) {
-        L++;
-        TRY(axbc_batch_levels_alloc(c, L + 2));
-        uint32_t *fprev = c->fmask[L - 1], *fcur = c->fmask[L];
-        CU(cudaMemsetAsync(fcur, 0, n * 4, s));
-        CU(cudaMemsetAsync((char *)c->bi + lvl_off, 0, lvl_len, s));
-        const bool push = (double)front * c->push_factor_batch < (double)unvis;
-        {
-            ProfScope ps(c, push ? KP_FWD_PUSH : KP_FWD_PULL, dte[L - 1] * (4.0 / W + 4.0));
-            CU(cudaMemsetAsync(c->task_ctr, 0, 4, s));
-            if (push)
-                k_fwd_push_m<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, fprev, fcur, c->seen, c->msigma,
-                                                        c->task_ctr);
-            else
-                k_fwd_pull_m<<<dgrid, BATCH_TPB, 0, s>>>(g->rev, srcmask, fprev, fcur, c->seen,
-                                                        c->msigma, c->task_ctr);
-        }
-        {
-            ProfScope ps(c, KP_LEVEL_STATS, (double)n * 16.0);
-            k_level_stats<<<grid, BATCH_TPB, 0, s>>>(n, srcmask, fcur, c->seen, g->fwd.col,
-                                                     g->rev.col, g->reach, c->bi);
-        }
-        CU_LAUNCH("forward level");
-        CU(cudaMemcpyAsync((char *)c->bi_host + lvl_off, (char *)c->bi + lvl_off, lvl_len,
-                           cudaMemcpyDeviceToHost, s));
-        CU(cudaStreamSynchronize(s));
-        for (int i = 0; i < nsrc; i++) {
-            if (((alive >> i) & 1u) && c->bi_host->lvl_new[i] == 0) {
-                Ls[i] = L;
-                alive &= ~(1u << i);
+        TRY(axbc_batch_levels_alloc(c, launched + K + 2));
+        for (int i = 0; i < K; i++) {
+            if (!prof) {
+                CU(cudaGraphLaunch(c->fwd_step_exec, s));
+            } else {
+                const int L = launched + i + 1;
+                {
+                    ProfScope ps(c, KP_FWD_PULL, 0);
+                    c->prof.back().tag = L;
+                    k_fwd_step<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, g->rev, c->bi, c->fmtab, c->seen,
+                                                           c->msigma, c->ctrs, ll);
+                }
+                {
+                    ProfScope ps(c, KP_LEVEL_STATS, 0);
+                    c->prof.back().tag = L;
+                    k_stats_step<<<sgrid, BATCH_TPB, 0, s>>>(n, c->bi, c->fmtab, c->seen, g->fwd.col,
+                                                             g->rev.col, g->reach, ll);
+                }
+                k_level_advance<<<1, 32, 0, s>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode,
+                                                 ll, c->lpool_cap, lmax);
+                c->launches++;
             }
         }
-        front = c->bi_host->front_deg;
-        unvis = c->bi_host->unvis_deg;
-        double cnt = 0;
-        for (int i = 0; i < nsrc; i++) cnt += (double)c->bi_host->lvl_new[i];
-        dte.push_back((double)c->bi_host->lvl_te);
-        dcnt.push_back(cnt);
-        if (!c->bi_host->any_new) break;
+        CU_LAUNCH("forward levels");
+        if (!prof) c->launches += 3ull * K;
+        launched += K;
+        c->prev_lend = std::min(launched, (int)c->fmask.size() - 1);  // masks written so far
+        CU(cudaMemcpyAsync((char *)c->bi_host + ctl_off, (char *)c->bi + ctl_off, ctl_len,
+                           cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        if (!c->bi_host->alive) break;
+        if (launched + 2 * K + 2 > AXBC_MAX_LEVELS) {
+            axbc_set_error("traversal deeper than %d levels", AXBC_MAX_LEVELS - 2);
+            return AXBC_ERR_RANGE;
+        }
+        K = std::min(2 * K, 256);
     }
-    // every pivot's frontier is empty at level L; its deepest depth is Ls-1
-    const int Dmax = L - 1;
-    uint32_t depth0 = 0;
-    for (int i = 0; i < nsrc; i++)
-        if (Ls[i] == 2) depth0 |= 1u << i;
-    CU(cudaMemcpyAsync(&c->bi->depth0mask, &depth0, 4, cudaMemcpyHostToDevice, s));
+    const int L = c->bi_host->lend, Dmax = c->bi_host->dmax;
 
-    for (int d = Dmax; d >= 0; d--) {
-        const uint32_t dmask = d >= 1 ? srcmask : depth0;
-        if (!dmask) continue;
-        double te_d = dte[d], cnt_d = dcnt[d];
-        if (d == 0) {
-            const double frac = (double)__builtin_popcount(dmask) / W;
-            te_d *= frac;
-            cnt_d *= frac;
+    // per-level totals for the byte model of the profiling hooks
+    std::vector<unsigned long long> lte, lcnt;
+    std::vector<int32_t> lmode;
+    if (prof) {
+        lte.resize(L + 1);
+        lcnt.resize(L + 1);
+        lmode.resize(L + 1);
+        CU(cudaMemcpy(lte.data(), c->d_level_te, (L + 1) * 8, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(lcnt.data(), c->d_level_cnt, (L + 1) * 8, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(lmode.data(), c->d_level_mode, (L + 1) * 4, cudaMemcpyDeviceToHost));
+        const double W = nsrc;
+        for (size_t i = prof_first; i < c->prof.size(); i++) {
+            ProfRec &r = c->prof[i];
+            if (r.tag < 1 || r.tag > L) continue;  // steps past the last level: no work
+            if (r.kind == KP_FWD_PULL) {
+                if (lmode[r.tag]) r.kind = KP_FWD_PUSH;
+                r.bytes = (double)lte[r.tag - 1] * (4.0 / W + 4.0);
+            } else if (r.kind == KP_LEVEL_STATS) {
+                r.bytes = (double)n * 16.0;
+            }
         }
-        const double bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
-        {
-            ProfScope ps(c, KP_BWD, bytes);
-            CU(cudaMemsetAsync(c->task_ctr, 0, 4, s));
-            k_bwd_m<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, dmask, d == Dmax, c->fmask[d],
-                                                c->fmask[d + 1], c->msigma, c->mdelta, c->mq,
-                                                c->mpartial, g->reach, c->task_ctr);
-        }
-        if (g->fwd.n_heavy) {
-            ProfScope ps(c, KP_BWD_COMBINE, 0);
-            k_bwd_combine_m<<<(g->fwd.n_heavy + 7) / 8, 256, 0, s>>>(
-                g->fwd, dmask, c->fmask[d], c->msigma, c->mdelta, c->mq, c->mpartial, g->reach);
-        }
-        CU_LAUNCH("backward level");
     }
+
+    // backward: depths Dmax .. 0 (depth 0 only for pivots whose BFS ended at level 2)
+    uint32_t depth0 = 0;
+    if (Dmax >= 0) {
+        for (int d = Dmax; d >= 0; d--) {
+            if (!prof) {
+                CU(cudaGraphLaunch(c->bwd_step_exec, s));
+                c->launches += g->fwd.n_heavy ? 3 : 2;
+                continue;
+            }
+            if (d == Dmax) {
+                CU(cudaMemcpy(&depth0, &c->bi->depth0mask, 4, cudaMemcpyDeviceToHost));
+            }
+            const double W = nsrc;
+            double te_d = (double)lte[d], cnt_d = (double)lcnt[d];
+            if (d == 0) {
+                const double frac = (double)__builtin_popcount(depth0) / W;
+                te_d *= frac;
+                cnt_d *= frac;
+            }
+            const double bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
+            {
+                ProfScope ps(c, KP_BWD, bytes);
+                k_bwd_step<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
+                                                       c->mq, c->mpartial, g->reach, c->ctrs, ll);
+            }
+            if (g->fwd.n_heavy) {
+                ProfScope ps(c, KP_BWD_COMBINE, 0);
+                k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, s>>>(
+                    g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach);
+            }
+            k_bwd_advance<<<1, 1, 0, s>>>(c->bi);
+            c->launches++;
+        }
+        CU_LAUNCH("backward levels");
+    }
+    CU(cudaMemcpyAsync(c->bi_host->Ls, c->bi->Ls, sizeof(c->bi_host->Ls), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(&c->bi_host->pool_short, &c->bi->pool_short, 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
     c->last_batch_levels = L;
     c->last_batch_nsrc = nsrc;
-    for (int i = 0; i < AXBC_W; i++) c->last_Ls[i] = i < nsrc ? Ls[i] : 0;
+    c->prev_lend = L;
+    c->pool_short = c->bi_host->pool_short != 0;
+    for (int i = 0; i < AXBC_W; i++) c->last_Ls[i] = i < nsrc ? c->bi_host->Ls[i] : 0;
     return AXBC_OK;
 }
 

@@ -131,12 +131,27 @@ struct BatchInfo {  // device, one multi-source batch
     // per-level scratch read back by the host
     unsigned long long lvl_new[AXBC_W];
     unsigned long long front_deg;
-    unsigned long long unvis_deg;
+    unsigned long long unvis_deg;   // in-degree sum of vertices some pivot has not seen
+    unsigned long long unvis_dec;   // this level's decrease of unvis_deg
     unsigned long long lvl_te;  // degree sum over the level's new (vertex, pivot) pairs
     uint32_t any_new;
     uint32_t task_ctr[4];
     int32_t H;
+    // device-driven level loop: the step kernels read their level and
+    // direction here, the advance kernels move them on
+    int32_t cur;        // last completed forward level
+    int32_t alive;      // 1 while the last completed level discovered vertices
+    int32_t lend;       // first level that discovered nothing (once alive == 0)
+    int32_t dmax;       // deepest depth = lend - 1
+    int32_t bd;         // next backward depth (counts down to -1)
+    int32_t push_next;  // 1: the next forward level pushes from the frontier
+    double push_factor;
+    int32_t Ls[AXBC_W];  // per pivot: first level that discovered nothing
+    int32_t pool_short;  // a level's list was capped by the pool's size
 };
+
+// capacity of the per-level tables of a context (levels of one traversal)
+#define AXBC_MAX_LEVELS (1 << 16)
 
 struct SamplerState;  // sampler.cu
 
@@ -159,6 +174,7 @@ struct ProfRec {
     int kind;
     double bytes;  // algorithmic bytes of the launch
     cudaEvent_t a, b;
+    int tag;       // forward level of a device-driven step (-1: none)
 };
 
 struct axbc_ctx {
@@ -188,6 +204,18 @@ struct axbc_ctx {
     float *mpartial = nullptr;      // heavy items * 32
     BatchInfo *bi = nullptr;
     BatchInfo *bi_host = nullptr;  // pinned
+    uint32_t **fmtab = nullptr;               // device copy of the fmask pointers
+    uint32_t *ctrs = nullptr;                 // per-level work counters (2 per level)
+    unsigned long long *d_level_te = nullptr;   // per level: degree sum of new pairs
+    unsigned long long *d_level_cnt = nullptr;  // per level: new (vertex, pivot) pairs
+    int32_t *d_level_mode = nullptr;            // per level: 1 push, 0 pull
+    uint32_t *lpool = nullptr;                  // per-level vertex lists
+    uint32_t *lstart = nullptr, *lcount = nullptr, *lcap = nullptr;
+    uint32_t lpool_cap = 0;
+    bool pool_short = false;  // the last batch ran out of list space
+    int prev_lend = 0;        // levels of the last batch whose masks need clearing
+    cudaGraphExec_t fwd_step_exec = nullptr;  // captured forward level step
+    cudaGraphExec_t bwd_step_exec = nullptr;  // captured backward level step
     int last_batch_levels = 0;
     int last_batch_nsrc = 0;
     int last_Ls[AXBC_W] = {0};  // first empty level of each pivot of the last batch
