@@ -106,7 +106,7 @@ PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bw
               "batch_bwd_combine", "batch_update", "sampler", "plain_fwd", "plain_bwd",
               "plain_other"]
 # kernel names behind each profiling kind (for matching ncu launch lists)
-PROF_KERNELS = {"batch_fwd_push": "k_fwd_step", "batch_fwd_pull": "k_fwd_step",
+PROF_KERNELS = {"batch_fwd_push": "k_fwd_push_step", "batch_fwd_pull": "k_fwd_pull_step",
                 "batch_level_stats": "k_stats_step", "batch_bwd": "k_bwd_step",
                 "batch_bwd_combine": "k_bwd_combine_step", "batch_update": "k_update_m",
                 "sampler": "k_sampler", "plain_fwd": "k_fwd_push1", "plain_bwd": "k_bwd1",

@@ -16,6 +16,11 @@
 
 static __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * AXBC_W; }
 
+// resident blocks per SM the pull kernel is compiled for (its register budget)
+#ifndef AXBC_PULL_MIN_BLOCKS
+#define AXBC_PULL_MIN_BLOCKS 6
+#endif
+
 // Per-level vertex lists: the vertices whose level-L mask is nonzero, appended
 // by the forward kernels that set the mask.  A level whose list would exceed
 // its capacity keeps counting but stops storing (count > cap: no list), and
@@ -50,7 +55,7 @@ __global__ void k_clean_levels(uint32_t *const *__restrict__ tab, const uint32_t
 }
 
 // roots: depth 0, sigma 1 (set_mlp_cuda, src/cuda_kernels.cu:862-876)
-__global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, uint32_t *seen,
+__global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t *fmask0, uint32_t *seen,
                              uint32_t *msigma, const uint32_t *__restrict__ col,
                              const uint32_t *__restrict__ rcol, unsigned long long m,
                              double push_factor, unsigned long long *level_te,
@@ -60,8 +65,8 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, u
     const int s = threadIdx.x;
     if (s == 0) {
         bi->nsrc = nsrc;
-        bi->napply = nsrc;
         bi->srcmask = nsrc >= 32 ? FULL_MASK : ((1u << nsrc) - 1u);
+        bi->applymask = bi->srcmask;
         bi->depth0mask = 0;
         bi->H = H;
         bi->cur = 0;
@@ -99,6 +104,7 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, uint32_t *fmask0, u
         rd += __shfl_xor_sync(FULL_MASK, rd, o);
     }
     if (s < nsrc) ll.pool[s] = bi->root[s];
+    if (s < AXBC_W) bi->lane_bc[s] = bc;
     if (s == 0) {
         // a vertex counts as unvisited until every pivot has seen it: with one
         // pivot its root is fully seen at once
@@ -187,6 +193,65 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
     }
 }
 
+// Push from up to 32 light frontier vertices at once, one per lane (f_l = 0:
+// none), edge-parallel: the warp walks the concatenation of their adjacency
+// lists 32 positions at a time, so a chunk of low-degree vertices costs one
+// pass instead of one pass per vertex.  Lane e finds its vertex by a binary
+// search over the inclusive degree prefix held across the lanes.
+__device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, uint32_t f_l,
+                                             const uint32_t *__restrict__ seen, uint32_t *fcur,
+                                             uint32_t *msigma, const LevelLists &ll, int L)
+{
+    const unsigned lane = lane_id();
+    uint32_t b = 0, d = 0;
+    if (f_l) {
+        b = a.col[v_l];
+        d = a.col[v_l + 1] - b;
+    }
+    uint32_t inc = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL_MASK, inc, o);
+        if ((int)lane >= o) inc += t;
+    }
+    const uint32_t total = __shfl_sync(FULL_MASK, inc, 31);
+    const uint32_t shift = b - (inc - d);  // position of concatenated index e: shift_k + e
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t e = base + lane;
+        uint32_t k = 0;  // lanes whose inclusive prefix is <= e
+#pragma unroll
+        for (int step = 16; step; step >>= 1)
+            if (__shfl_sync(FULL_MASK, inc, k + step - 1) <= e) k += step;
+        const uint32_t pk = __shfl_sync(FULL_MASK, shift, k) + e;
+        const uint32_t fk = __shfl_sync(FULL_MASK, f_l, k);
+        uint32_t u = 0, nm = 0;
+        if (e < total) {
+            u = a.row[pk];
+            nm = fk & ~seen[u];
+        }
+        const uint32_t old = nm ? atomicOr(&fcur[u], nm) : 1u;
+        list_append(ll, L, old == 0u, u);
+        unsigned act = __ballot_sync(FULL_MASK, nm != 0);
+        while (act) {
+            // up to 4 edges: gather the parents' sigma rows, then add
+            uint32_t uu[4], mm[4], sg[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int j = act ? __ffs(act) - 1 : 0;
+                const bool ok = act != 0;
+                act &= act - 1;
+                uu[q] = __shfl_sync(FULL_MASK, u, j);
+                mm[q] = ok ? __shfl_sync(FULL_MASK, nm, j) : 0u;
+                const uint32_t vj = __shfl_sync(FULL_MASK, v_l, __shfl_sync(FULL_MASK, k, j));
+                sg[q] = ((mm[q] >> lane) & 1u) ? msigma[row_base(vj) + lane] : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if ((mm[q] >> lane) & 1u) atomicAdd(&msigma[row_base(uu[q]) + lane], sg[q]);
+        }
+    }
+}
+
 __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__restrict__ fprev,
                                               uint32_t *fcur, const uint32_t *__restrict__ seen,
                                               uint32_t *msigma, uint32_t *ctr, const LevelLists &ll,
@@ -215,14 +280,7 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
                 v_l = lst[i];
                 if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fprev[v_l];
             }
-            unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
-            while (act) {
-                const int j = __ffs(act) - 1;
-                act &= act - 1;
-                const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
-                const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
-                push_span(a, v, f, a.col[v], a.col[v + 1], seen, fcur, msigma, ll, L);
-            }
+            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
@@ -233,69 +291,148 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
                 v_l = a.order[beg + lane];
                 f_l = fprev[v_l];
             }
-            unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
-            while (act) {
-                const int j = __ffs(act) - 1;
-                act &= act - 1;
-                const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
-                const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
-                push_span(a, v, f, a.col[v], a.col[v + 1], seen, fcur, msigma, ll, L);
-            }
+            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L);
         }
     }
 }
 
 // Forward level L, pull into vertex u for the pivots `ns` that have not seen
-// it: sum sigma_s over every in-neighbour at depth L-1 from pivot s.  The
-// positions of a 32-wide chunk are staged in shared memory and their gathers
-// issued eight at a time before any is consumed.
+// it: sum sigma_s over every in-neighbour at depth L-1 from pivot s (u32 sums:
+// any order gives the same bits).  The positions of a 32-wide chunk are staged
+// in shared memory; each 8-position group with a hit issues its eight gathers
+// before any is consumed.
 __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32_t b0, uint32_t b1,
                                               const uint32_t *__restrict__ fprev,
                                               const uint32_t *__restrict__ msigma, uint32_t *su,
                                               uint32_t *sg, uint32_t &acc)
 {
     const unsigned lane = lane_id();
-    bool found = false;
+    const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
+    const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
+    uint32_t found = 0;
     acc = 0;
+    // the next chunk's adjacency entries load while this chunk is consumed
+    uint32_t vn = b0 + lane < b1 ? rv.row[b0 + lane] : 0u;
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
-        uint32_t v = 0, fm = 0;
-        if (e < b1) {
-            v = rv.row[e];
-            fm = fprev[v] & ns;
-        }
-        unsigned act = __ballot_sync(FULL_MASK, fm != 0);
+        const uint32_t v = vn;
+        vn = e + 32 < b1 ? rv.row[e + 32] : 0u;
+        const uint32_t fm = e < b1 ? fprev[v] & ns : 0u;
+        const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
+        found |= __reduce_or_sync(FULL_MASK, fm);
         su[lane] = v;
         sg[lane] = fm;
         __syncwarp();
-        while (act) {
+#pragma unroll 1
+        for (int g = 0; g < 4; g++) {
+            if (!((act >> (8 * g)) & 0xffu)) continue;
             uint32_t x[8];
-            bool h[8];
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int j = act ? __ffs(act) - 1 : 0;
-                const bool ok = act != 0;
-                act &= act - 1;
-                h[q] = ok && ((sg[j] >> lane) & 1u);
-                x[q] = h[q] ? msigma[row_base(su[j]) + lane] : 0u;
+            for (int h = 0; h < 2; h++) {
+                const uint4 ua = su4[2 * g + h], ga = sg4[2 * g + h];
+                const uint32_t u[4] = {ua.x, ua.y, ua.z, ua.w};
+                const uint32_t m[4] = {ga.x, ga.y, ga.z, ga.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    x[4 * h + q] = ((m[q] >> lane) & 1u) ? msigma[row_base(u[q]) + lane] : 0u;
             }
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
+            for (int q = 0; q < 8; q++) acc += x[q];
+        }
+        __syncwarp();
+    }
+    return found;
+}
+
+// Pull into up to 32 light vertices at once, one per lane (pivots ns_l; 0:
+// none), edge-parallel over the concatenation of their in-adjacency lists:
+// lane e finds its vertex by a binary search over the inclusive degree prefix
+// held across the lanes.  Positions arrive grouped by vertex, so one running
+// sum per lane (pivot) is written out whenever the vertex changes.  Returns the
+// discovered mask of the lane's own vertex.
+__device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, uint32_t ns_l,
+                                                 const uint32_t *__restrict__ fprev, uint32_t *msigma,
+                                                 uint32_t *su, uint32_t *sg, uint32_t *sk)
+{
+    const unsigned lane = lane_id();
+    uint32_t b = 0, d = 0;
+    if (ns_l) {
+        b = rv.col[u_l];
+        d = rv.col[u_l + 1] - b;
+    }
+    uint32_t inc = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL_MASK, inc, o);
+        if ((int)lane >= o) inc += t;
+    }
+    const uint32_t total = __shfl_sync(FULL_MASK, inc, 31);
+    const uint32_t shift = b - (inc - d);  // position of concatenated index e: shift_k + e
+    uint32_t mine = 0, acc = 0, fo = 0;
+    int cur = -1;
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t e = base + lane;
+        uint32_t k = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1)
+            if (__shfl_sync(FULL_MASK, inc, k + step - 1) <= e) k += step;
+        const uint32_t pk = __shfl_sync(FULL_MASK, shift, k) + e;
+        const uint32_t nk = __shfl_sync(FULL_MASK, ns_l, k);
+        uint32_t v = 0, fm = 0;
+        if (e < total) {
+            v = rv.row[pk];
+            fm = fprev[v] & nk;
+        }
+        const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
+        if (!act) continue;
+        su[lane] = v;
+        sg[lane] = fm;
+        sk[lane] = k;
+        __syncwarp();
+#pragma unroll 1
+        for (int g = 0; g < 8; g++) {
+            if (!((act >> (4 * g)) & 0xfu)) continue;
+            uint32_t x[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t m = sg[4 * g + q];
+                x[q] = ((m >> lane) & 1u) ? msigma[row_base(su[4 * g + q]) + lane] : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t m = sg[4 * g + q];
+                if (!m) continue;
+                const int kq = (int)sk[4 * g + q];
+                if (kq != cur) {
+                    if (cur >= 0) {
+                        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+                        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
+                        if ((int)lane == cur) mine = fo;
+                    }
+                    cur = kq;
+                    acc = 0;
+                    fo = 0;
+                }
                 acc += x[q];
-                found |= h[q];
+                fo |= m;
             }
         }
         __syncwarp();
     }
-    return __ballot_sync(FULL_MASK, found);
+    if (cur >= 0) {
+        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
+        if ((int)lane == cur) mine = fo;
+    }
+    return mine;
 }
 
 __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
                                               const uint32_t *__restrict__ fprev, uint32_t *fcur,
                                               const uint32_t *__restrict__ seen, uint32_t *msigma,
                                               uint32_t *ctr, uint32_t *su, uint32_t *sg,
-                                              const LevelLists &ll, int L)
+                                              uint32_t *sk, const LevelLists &ll, int L)
 {
     const unsigned lane = lane_id();
     const uint64_t nhi = rv.n_heavy_items, nu = n_units(rv);
@@ -322,21 +459,9 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
             uint32_t u_l = 0, ns_l = 0;
             if (lane < cnt) {
                 u_l = rv.order[beg + lane];
-                if (rv.col[u_l + 1] > rv.col[u_l]) ns_l = srcmask & ~seen[u_l];
+                ns_l = srcmask & ~seen[u_l];
             }
-            unsigned act = __ballot_sync(FULL_MASK, ns_l != 0);
-            uint32_t mine = 0;
-            while (act) {
-                const int j = __ffs(act) - 1;
-                act &= act - 1;
-                const uint32_t u = __shfl_sync(FULL_MASK, u_l, j);
-                const uint32_t ns = __shfl_sync(FULL_MASK, ns_l, j);
-                uint32_t acc;
-                const uint32_t nm =
-                    pull_span(rv, ns, rv.col[u], rv.col[u + 1], fprev, msigma, su, sg, acc);
-                if ((nm >> lane) & 1u) msigma[row_base(u) + lane] = acc;
-                if ((int)lane == j) mine = nm;
-            }
+            const uint32_t mine = pull_light32(rv, u_l, ns_l, fprev, msigma, su, sg, sk);
             if (mine) fcur[u_l] = mine;
             list_append(ll, L, mine != 0u, u_l);
         }
@@ -344,20 +469,34 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
 }
 
 // One forward level, device-driven: the level is bi->cur + 1 and the direction
-// bi->push_next (set by the previous k_level_advance); a no-op once a level
-// discovered nothing.
-__global__ void __launch_bounds__(BATCH_TPB, 8) k_fwd_step(Adj a, Adj rv, const BatchInfo *__restrict__ bi,
-                                                        uint32_t *const *__restrict__ tab,
-                                                        const uint32_t *__restrict__ seen,
-                                                        uint32_t *msigma, uint32_t *ctrs,
-                                                        LevelLists ll)
+// bi->push_next (set by the previous k_level_advance).  Both direction kernels
+// are launched every level; the one not chosen returns at once, as both do
+// once a level discovered nothing.
+__global__ void __launch_bounds__(BATCH_TPB, 8) k_fwd_push_step(Adj a, const BatchInfo *__restrict__ bi,
+                                                             uint32_t *const *__restrict__ tab,
+                                                             const uint32_t *__restrict__ seen,
+                                                             uint32_t *msigma, uint32_t *ctrs,
+                                                             LevelLists ll)
 {
-    __shared__ uint32_t s_u[BATCH_TPB], s_g[BATCH_TPB];
-    if (!bi->alive) return;
+    if (!bi->alive || !bi->push_next) return;
     const int L = bi->cur + 1;
-    uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
-    if (bi->push_next) fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L);
-    else fwd_pull_body(rv, bi->srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, su, sg, ll, L);
+    fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L);
+}
+
+__global__ void __launch_bounds__(BATCH_TPB, AXBC_PULL_MIN_BLOCKS) k_fwd_pull_step(Adj rv, const BatchInfo *__restrict__ bi,
+                                                             uint32_t *const *__restrict__ tab,
+                                                             const uint32_t *__restrict__ seen,
+                                                             uint32_t *msigma, uint32_t *ctrs,
+                                                             LevelLists ll)
+{
+    __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
+    __shared__ uint32_t s_k[BATCH_TPB];
+    if (!bi->alive || bi->push_next) return;
+    const int L = bi->cur + 1;
+    const unsigned w0 = threadIdx.x & ~31u;
+    fwd_pull_body(rv, bi->srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, s_u + w0, s_g + w0,
+                  s_k + w0, ll, L);
 }
 
 // After level L = bi->cur + 1: fold the level mask into `seen` and count, per
@@ -533,13 +672,13 @@ __device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, ui
     const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
     const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
     float P = 0.0f;
+    // the next chunk's adjacency entries load while this chunk is consumed
+    uint32_t un = b0 + lane < b1 ? a.row[b0 + lane] : 0u;
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
-        uint32_t u = 0, gm = 0;
-        if (e < b1) {
-            u = a.row[e];
-            gm = fnext[u] & f;
-        }
+        const uint32_t u = un;
+        un = e + 32 < b1 ? a.row[e + 32] : 0u;
+        const uint32_t gm = e < b1 ? fnext[u] & f : 0u;
         const unsigned pm = __ballot_sync(FULL_MASK, gm != 0);
         if (!pm) continue;
         su[lane] = u;
@@ -700,71 +839,135 @@ __global__ void k_bwd_advance(BatchInfo *bi)
     if (bi->bd >= 0) bi->bd--;
 }
 
-// bc update for pivots 0..napply-1 in order (update_bc, src/cuda_kernels.cu:
-// 269-286).  A pivot that did not reach v contributes delta = reach[v].  Zero
-// terms are skipped: x + float(0/p) == x for p > 0.
-__global__ void __launch_bounds__(BATCH_TPB) k_update_m(float *bc, const float *__restrict__ mdelta,
-                                                        const uint32_t *__restrict__ seen,
-                                                        const uint32_t *__restrict__ reach,
-                                                        uint64_t n, const BatchInfo *__restrict__ bi)
+// bc update for the applied pivots in lane order (update_bc, src/cuda_kernels.cu:
+// 269-286), each into its lane's bc vector.  A pivot that did not reach v
+// contributes delta = reach[v].  Zero terms are skipped: x + float(0/p) == x for
+// p > 0.  One thread per vertex, its 32 dependencies read from rows a warp
+// staged in shared memory.
+// 4-byte global -> shared copies that bypass registers (cp.async), so a warp
+// keeps up to 32 row loads of one chunk and the next chunk's in flight
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 {
-    __shared__ uint32_t s_root[AXBC_W], s_reach[AXBC_W];
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// stage the dependency rows of the chunk's reached vertices: lane l copies
+// column l of each row
+__device__ __forceinline__ void stage_rows(float (*rows)[33], const float *__restrict__ mdelta,
+                                           uint64_t base, uint32_t sv)
+{
+    const unsigned lane = lane_id();
+    unsigned need = __ballot_sync(FULL_MASK, sv != 0u);
+    while (need) {
+        const int r = __ffs(need) - 1;
+        need &= need - 1;
+        cp_async4(&rows[r][lane], mdelta + row_base(base + r) + lane);
+    }
+    cp_async_commit();
+}
+
+#define UPD_TPB 128  // 34 KB of staged rows per block
+__global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ mdelta,
+                                                      const uint32_t *__restrict__ seen,
+                                                      const uint32_t *__restrict__ reach, uint64_t n,
+                                                      const BatchInfo *__restrict__ bi)
+{
+    __shared__ uint32_t s_root[AXBC_W], s_reach[AXBC_W], s_skip0[AXBC_W];
     __shared__ double s_p[AXBC_W];
     __shared__ unsigned long long s_nvt[AXBC_W];
     __shared__ InvSplit s_iv[AXBC_W];
-    const uint32_t napply = bi->napply;
+    __shared__ float *s_bc[AXBC_W];
+    // per warp, two chunks: the dependency rows of 32 vertices, padded to 33
+    // floats so that thread t reading row t, column s hits bank (t + s) mod 32
+    __shared__ float s_rows[UPD_TPB / 32][2][32][33];
+    const uint32_t amask = bi->applymask & bi->srcmask;
     if (threadIdx.x < AXBC_W) {
         const int s = threadIdx.x;
-        if (s < (int)napply) {
+        s_bc[s] = bi->lane_bc[s];
+        if ((amask >> s) & 1u) {
             const uint32_t r = bi->root[s];
             const uint32_t rv = reach[r];
             const uint32_t all = (bi->H == 1 ? (uint32_t)bi->rsum[s] : 0u) + rv;
             s_root[s] = r;
             s_reach[s] = rv;
             s_p[s] = bi->p[s];
+            s_skip0[s] = bi->p[s] > 0.0;
             s_nvt[s] = bi->nvis[s] + all;
             s_iv[s] = inv_split(bi->p[s]);
         } else {
             s_root[s] = 0xffffffffu;
             s_reach[s] = 0;
             s_p[s] = 1.0;
+            s_skip0[s] = 1;
             s_nvt[s] = 2;
             s_iv[s] = inv_split(1.0);
         }
     }
     __syncthreads();
-    if (napply == 0) return;
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-         v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t sv = seen[v];
-        const uint32_t rv = reach[v];
-        if (sv == 0 && rv == 0) {
-            // unreached by every pivot with delta 0: only a root term could
-            // apply, and roots are reached
-            continue;
+    if (amask == 0) return;
+    const int slast = 31 - __clz(amask);
+    const unsigned lane = lane_id();
+    const unsigned wid = threadIdx.x >> 5;
+    const uint64_t stride = (uint64_t)gridDim.x * (UPD_TPB / 32) * 32;
+    uint64_t base = (blockIdx.x * (uint64_t)(UPD_TPB / 32) + wid) * 32;
+    if (base >= n) return;
+    uint32_t sv = 0, rv = 0;
+    if (base + lane < n) {
+        sv = seen[base + lane];
+        rv = reach[base + lane];
+    }
+    stage_rows(s_rows[wid][0], mdelta, base, sv);
+    for (int buf = 0; base < n; base += stride, buf ^= 1) {
+        // the next chunk's rows load while this chunk is summed
+        const uint64_t next = base + stride;
+        uint32_t svn = 0, rvn = 0;
+        if (next + lane < n) {
+            svn = seen[next + lane];
+            rvn = reach[next + lane];
         }
-        const float rf = __uint2float_rn(rv);
-        const float4 *row = reinterpret_cast<const float4 *>(mdelta + row_base(v));
-        float b = bc[v];
-        for (int q = 0; q < AXBC_W / 4; q++) {
-            if (4 * q >= (int)napply) break;
-            float4 x = make_float4(rf, rf, rf, rf);
-            if ((sv >> (4 * q)) & 0xfu) x = row[q];
-            const float dq[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int s = 4 * q + k;
-                if (s >= (int)napply) break;
+        if (next < n) {
+            stage_rows(s_rows[wid][buf ^ 1], mdelta, next, svn);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        const uint64_t v = base + lane;
+        // unreached by every pivot with delta 0: only a root term could apply,
+        // and roots are reached
+        if (sv != 0u || rv != 0u) {
+            const float(*rows)[33] = s_rows[wid][buf];
+            const float rf = __uint2float_rn(rv);
+            // lanes in order; consecutive lanes of one run add into one
+            // register, written back when the target vector changes
+            float *tgt = nullptr;
+            float b = 0.0f;
+            for (int s = 0; s <= slast; s++) {
+                if (!((amask >> s) & 1u)) continue;
+                if (s_bc[s] != tgt) {
+                    if (tgt) tgt[v] = b;
+                    tgt = s_bc[s];
+                    b = tgt[v];
+                }
                 if ((uint32_t)v == s_root[s]) {
                     if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
                     continue;
                 }
-                const float dv = ((sv >> s) & 1u) ? dq[k] : rf;
-                if (dv == 0.0f && s_p[s] > 0.0) continue;
+                const float dv = ((sv >> s) & 1u) ? rows[lane][s] : rf;
+                if (dv == 0.0f && s_skip0[s]) continue;
                 b = __fadd_rn(b, bc_term_fast(dv, s_reach[s], s_p[s], s_iv[s]));
             }
+            tgt[v] = b;
         }
-        bc[v] = b;
+        __syncwarp();
+        sv = svn;
+        rv = rvn;
     }
 }
 
@@ -772,11 +975,14 @@ __global__ void __launch_bounds__(BATCH_TPB) k_update_m(float *bc, const float *
 __global__ void k_extract_delta(float *out, const float *__restrict__ mdelta,
                                 const uint32_t *__restrict__ seen,
                                 const uint32_t *__restrict__ reach, uint64_t n,
-                                const BatchInfo *__restrict__ bi)
+                                const BatchInfo *__restrict__ bi, int lane_lo, int lane_hi)
 {
-    const uint32_t napply = bi->napply;
-    if (napply == 0) return;
-    const int s = napply - 1;
+    // the highest applied lane of [lane_lo, lane_hi)
+    uint32_t range = lane_hi >= 32 ? FULL_MASK : ((1u << lane_hi) - 1u);
+    range &= ~((1u << lane_lo) - 1u);
+    const uint32_t am = bi->applymask & bi->srcmask & range;
+    if (am == 0) return;
+    const int s = 31 - __clz(am);
     const uint32_t root = bi->root[s];
     const bool root_done = (bi->depth0mask >> s) & 1u;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
@@ -880,12 +1086,20 @@ static int dyn_grid(axbc_ctx *c)
 {
     // dynamic kernels: as many blocks as stay resident; work comes from counters
     if (!c->dyn_blocks_per_sm) {
-        int a = 0, b = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_step, BATCH_TPB, 0));
+        int a = 0, b = 0, d = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_step, BATCH_TPB, 0));
         CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_fwd_pull_step, BATCH_TPB, 0));
         c->dyn_blocks_per_sm = std::max(1, std::min(a, b));
+        c->pull_blocks_per_sm = std::max(1, d);
     }
     return axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm);
+}
+
+static int pull_grid(axbc_ctx *c)
+{
+    dyn_grid(c);
+    return axbc_grid_for(c, BATCH_TPB, c->pull_blocks_per_sm);
 }
 
 // the kernels of one forward level / one backward depth, in stream order
@@ -893,8 +1107,10 @@ static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
 {
     axbc_graph *g = c->g;
     const LevelLists ll = lists_of(c);
-    k_fwd_step<<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, g->rev, c->bi, c->fmtab, c->seen, c->msigma,
-                                                   c->ctrs, ll);
+    k_fwd_push_step<<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->seen, c->msigma,
+                                                        c->ctrs, ll);
+    k_fwd_pull_step<<<pull_grid(c), BATCH_TPB, 0, c->stream>>>(g->rev, c->bi, c->fmtab, c->seen, c->msigma,
+                                                        c->ctrs, ll);
     k_stats_step<<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->fwd.col,
                                                      g->rev.col, g->reach, ll);
     k_level_advance<<<1, 32, 0, c->stream>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode,
@@ -979,7 +1195,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     const uint32_t lmax = list_max_of(c);
     {
         ProfScope ps(c, KP_LEVEL_STATS, 0);
-        k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->fmask[0], c->seen, c->msigma, g->fwd.col,
+        k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
                                       g->rev.col, g->m, c->push_factor_batch, c->d_level_te,
                                       c->d_level_cnt, ll, c->lpool_cap, lmax);
     }
@@ -997,10 +1213,16 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
             } else {
                 const int L = launched + i + 1;
                 {
+                    ProfScope ps(c, KP_FWD_PUSH, 0);
+                    c->prof.back().tag = L;
+                    k_fwd_push_step<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->seen,
+                                                                c->msigma, c->ctrs, ll);
+                }
+                {
                     ProfScope ps(c, KP_FWD_PULL, 0);
                     c->prof.back().tag = L;
-                    k_fwd_step<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, g->rev, c->bi, c->fmtab, c->seen,
-                                                           c->msigma, c->ctrs, ll);
+                    k_fwd_pull_step<<<pull_grid(c), BATCH_TPB, 0, s>>>(g->rev, c->bi, c->fmtab, c->seen,
+                                                                c->msigma, c->ctrs, ll);
                 }
                 {
                     ProfScope ps(c, KP_LEVEL_STATS, 0);
@@ -1014,7 +1236,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
             }
         }
         CU_LAUNCH("forward levels");
-        if (!prof) c->launches += 3ull * K;
+        if (!prof) c->launches += 4ull * K;
         launched += K;
         c->prev_lend = std::min(launched, (int)c->fmask.size() - 1);  // masks written so far
         CU(cudaMemcpyAsync((char *)c->bi_host + ctl_off, (char *)c->bi + ctl_off, ctl_len,
@@ -1043,9 +1265,10 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         for (size_t i = prof_first; i < c->prof.size(); i++) {
             ProfRec &r = c->prof[i];
             if (r.tag < 1 || r.tag > L) continue;  // steps past the last level: no work
-            if (r.kind == KP_FWD_PULL) {
-                if (lmode[r.tag]) r.kind = KP_FWD_PUSH;
-                r.bytes = (double)lte[r.tag - 1] * (4.0 / W + 4.0);
+            if (r.kind == KP_FWD_PUSH || r.kind == KP_FWD_PULL) {
+                // the byte model goes to the direction that ran; the other launch returned at once
+                const bool ran = (r.kind == KP_FWD_PUSH) == (lmode[r.tag] != 0);
+                r.bytes = ran ? (double)lte[r.tag - 1] * (4.0 / W + 4.0) : 0.0;
             } else if (r.kind == KP_LEVEL_STATS) {
                 r.bytes = (double)n * 16.0;
             }
@@ -1098,21 +1321,49 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     return AXBC_OK;
 }
 
-int axbc_batch_apply(axbc_ctx *c)
+// The update of the applied lanes into each lane's bc vector, then the last
+// applied dependency vector of each lane segment [lane_lo[i], lane_hi[i]) into
+// delta_out[i] (defaults: one segment of all lanes into the context's).
+int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo,
+                           const int *lane_hi, int nseg)
 {
     axbc_graph *g = c->g;
     cudaStream_t s = c->stream;
-    const int grid = axbc_grid_for(c, BATCH_TPB, 8);
+    // a grid-stride loop: exactly the blocks that stay resident
+    if (!c->upd_blocks_per_sm) {
+        int b = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_update_m, UPD_TPB, 0));
+        c->upd_blocks_per_sm = std::max(1, b);
+    }
+    const int grid = axbc_grid_for(c, UPD_TPB, c->upd_blocks_per_sm);
     {
         ProfScope ps(c, KP_UPDATE, (double)g->n * c->last_batch_nsrc * 20.0);
-        k_update_m<<<grid, BATCH_TPB, 0, s>>>(c->bc, c->mdelta, c->seen, g->reach, g->n, c->bi);
+        k_update_m<<<grid, UPD_TPB, 0, s>>>(c->mdelta, c->seen, g->reach, g->n, c->bi);
     }
-    {
+    for (int i = 0; i < nseg; i++) {
         ProfScope ps(c, KP_UPDATE, 0);
-        k_extract_delta<<<grid, 256, 0, s>>>(c->delta_last, c->mdelta, c->seen, g->reach, g->n, c->bi);
+        k_extract_delta<<<grid, 256, 0, s>>>(delta_out ? delta_out[i] : c->delta_last, c->mdelta,
+                                              c->seen, g->reach, g->n, c->bi,
+                                              lane_lo ? lane_lo[i] : 0, lane_hi ? lane_hi[i] : AXBC_W);
     }
     CU_LAUNCH("update");
     c->delta_last_valid = true;
+    return AXBC_OK;
+}
+
+int axbc_batch_apply(axbc_ctx *c) { return axbc_batch_apply_lanes(c, nullptr, nullptr, nullptr, 1); }
+
+__global__ void k_set_lane_targets(BatchInfo *bi, LaneTargets t)
+{
+    if (threadIdx.x < AXBC_W) bi->lane_bc[threadIdx.x] = t.bc[threadIdx.x];
+}
+
+int axbc_batch_set_targets(axbc_ctx *c, float *const *bc_of_lane)
+{
+    LaneTargets t;
+    for (int i = 0; i < AXBC_W; i++) t.bc[i] = bc_of_lane[i];
+    k_set_lane_targets<<<1, AXBC_W, 0, c->stream>>>(c->bi, t);
+    CU_LAUNCH("k_set_lane_targets");
     return AXBC_OK;
 }
 
@@ -1210,7 +1461,7 @@ __global__ void k_selftest_div(uint64_t n, uint64_t seed, unsigned long long *ba
         const uint64_t h1 = st_mix(seed ^ (i * 3 + 1)), h2 = st_mix(seed ^ (i * 3 + 2));
         float x;
         double p;
-        switch (i & 3) {
+        switch (i % 6) {
         case 0:  // pivot probabilities: 1/N-like and products of small integers
             x = (float)((h1 & 0xffffff) + 1) * ldexpf(1.0f, (int)((h1 >> 24) & 31) - 16);
             p = 1.0 / (double)((h2 & 0xffffff) + 1);
@@ -1226,9 +1477,20 @@ __global__ void k_selftest_div(uint64_t n, uint64_t seed, unsigned long long *ba
             x = (float)(target * p);
             break;
         }
-        default:  // integers times integers
+        case 3:  // integers times integers
             x = (float)((h1 & 0xfffff) + 1);
             p = (double)((h2 & 0xfff) + 1) / (double)((h2 >> 12 & 0xfffff) + 1);
+            break;
+        case 4:  // exact powers of two: small integers over p = 2^-k
+            x = (float)((h1 & 15) + 1) * ldexpf(1.0f, (int)((h1 >> 4) & 15) - 8);
+            p = ldexp(1.0, -(int)(h2 & 31));
+            break;
+        default: {  // just below a power of two, around the quarter-ulp boundary
+            p = (double)((h2 >> 11) + 1) * 0x1.0p-53 + 1e-9;
+            const double pw = ldexp(1.0, (int)(h1 & 31) - 8);
+            const double target = pw * (1.0 - 0x1.0p-26 * (1.0 + ((int)((h1 >> 5) & 15) - 8) * 0x1.0p-20));
+            x = (float)(target * p);
+        }
         }
         if (!(x > 0.0f) || !(p > 0.0)) continue;
         const InvSplit iv = inv_split(p);

@@ -133,7 +133,7 @@ int main(int argc, char **argv)
         case 's': seed = strtoll(optarg, nullptr, 10); break;
         case 'W':
             width = atoi(optarg);
-            if (width < 1 || width > AXBC_MAX_BATCH) die("Invalid batch width (-W): %s\n", optarg);
+            if (width < 1 || width > AXBC_MAX_WIDTH) die("Invalid batch width (-W): %s\n", optarg);
             break;
         default: usage(argv[0]);
         }

@@ -119,7 +119,7 @@ struct PivotCounters {  // device, single-source
 
 struct BatchInfo {  // device, one multi-source batch
     uint32_t nsrc;
-    uint32_t napply;      // sources whose update is applied (Bader replay)
+    uint32_t applymask;   // sources whose update is applied (Bader replay)
     uint32_t srcmask;
     uint32_t depth0mask;  // sources whose BFS ended at level 2
     uint32_t root[AXBC_W];
@@ -148,6 +148,13 @@ struct BatchInfo {  // device, one multi-source batch
     double push_factor;
     int32_t Ls[AXBC_W];  // per pivot: first level that discovered nothing
     int32_t pool_short;  // a level's list was capped by the pool's size
+    int32_t pad_;
+    float *lane_bc[AXBC_W];  // per pivot: the bc vector its update goes to
+};
+
+// the bc vector of each lane, for a pass whose lanes belong to several runs
+struct LaneTargets {
+    float *bc[AXBC_W];
 };
 
 // capacity of the per-level tables of a context (levels of one traversal)
@@ -247,6 +254,8 @@ struct axbc_ctx {
     uint64_t bytes = 0;
     int num_sms = 0;
     int dyn_blocks_per_sm = 0;  // resident blocks of the dynamic kernels
+    int upd_blocks_per_sm = 0;  // resident blocks of the batched bc update
+    int pull_blocks_per_sm = 0; // resident blocks of the forward pull kernel
 };
 
 // allocation with byte accounting
@@ -265,6 +274,9 @@ int axbc_single_update(axbc_ctx *c, uint32_t v0, double p, const uint32_t *reach
 int axbc_ensure_batch(axbc_ctx *c);
 int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H);
 int axbc_batch_apply(axbc_ctx *c);
+int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo,
+                           const int *lane_hi, int nseg);
+int axbc_batch_set_targets(axbc_ctx *c, float *const *bc_of_lane);
 int axbc_batch_levels_alloc(axbc_ctx *c, int levels);
 
 // grid sizing
@@ -336,9 +348,12 @@ __device__ __forceinline__ float div_to_float(float x, double p, InvSplit iv)
         const float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
         const uint32_t bits = __float_as_uint(s);
         const uint32_t ex = (bits >> 23) & 0xffu;
-        if (ex >= 40u && ex <= 210u && (bits & 0x7fffffu) != 0u) {
-            const float half_ulp = __uint_as_float((ex - 24u) << 23);
-            const float dist = fabsf(__fsub_rn(fabsf(err), half_ulp));
+        if (ex >= 40u && ex <= 210u) {
+            // the rounding boundary on err's side: half an ulp of s, or a
+            // quarter below a power of two (the spacing halves there)
+            const uint32_t sh = ((bits & 0x7fffffu) == 0u && err < 0.0f) ? 25u : 24u;
+            const float tie = __uint_as_float((ex - sh) << 23);
+            const float dist = fabsf(__fsub_rn(fabsf(err), tie));
             if (dist > __fmul_rn(s, 9.094947e-13f /* 2^-40 */)) return s;
         }
     }

@@ -29,9 +29,9 @@ struct SamplerState {
     int32_t nb;
     uint32_t napply;
     uint64_t skipped_run;
-    uint32_t v0[AXBC_W];
-    double p[AXBC_W];
-    uint64_t skip_before[AXBC_W];
+    uint32_t v0[AXBC_MAX_WIDTH];
+    double p[AXBC_MAX_WIDTH];
+    uint64_t skip_before[AXBC_MAX_WIDTH];
 };
 
 struct SamplerDists {
@@ -199,7 +199,7 @@ __global__ void k_sampler_init(SamplerState *ss, uint32_t *checks, int64_t seed,
 
 // Draw the rounds of one batch: up to W accepted pivots.
 __global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const uint32_t *checks,
-                          BatchInfo *bi, double S_lcc)
+                          double S_lcc)
 {
     ss->nb = 0;
     ss->napply = 0;
@@ -313,8 +313,6 @@ __global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const
         ss->v0[nb] = v0;
         ss->p[nb] = prob;
         ss->skip_before[nb] = skipped_run;
-        bi->root[nb] = v0;
-        bi->p[nb] = prob;
         skipped_run = 0;
         nb++;
         ui++;
@@ -327,15 +325,31 @@ __global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const
     ss->dropped += dropped;
 }
 
-// After the batch's traversal: replay Bader's test between its pivots, fix
-// how many are applied, and account rounds, skips and traversed edges.
+// Pivots [off, off + count) of a drawn round become lanes lane0 + 0.. of one
+// pass (count = min(nb - off, AXBC_W - lane0)).
+__global__ void k_load_pass(const SamplerState *ss, BatchInfo *bi, int off, int lane0)
+{
+    const int s = threadIdx.x;
+    const int count = min(ss->nb - off, AXBC_W - lane0);
+    if (s < count) {
+        bi->root[lane0 + s] = ss->v0[off + s];
+        bi->p[lane0 + s] = ss->p[off + s];
+    }
+}
+
+// After a pass (the drawn pivots [off, off + AXBC_W)): replay Bader's test
+// between its pivots, fix how many are applied, and account rounds, skips and
+// traversed edges.  The pass that ends the round also settles the degree-0
+// draws after its last pivot.
 __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__restrict__ bc,
                                const float *__restrict__ mdelta, const uint32_t *__restrict__ seen,
                                const uint32_t *__restrict__ reach, const uint32_t *__restrict__ checks,
-                               float *b, uint32_t *hist_v, double *hist_p, uint64_t hist_cap)
+                               float *b, uint32_t *hist_v, double *hist_p, uint64_t hist_cap,
+                               int off, int lane0)
 {
     if (ss->done && ss->nb == 0) return;
-    const int nb = ss->nb;
+    const int nb = max(0, min(ss->nb - off, AXBC_W - lane0));
+    const bool last = off + nb >= ss->nb;
     const uint64_t N = ss->N;
     const uint32_t c = ss->bader_c;
     const double lim = (double)((uint64_t)c * N);
@@ -346,7 +360,7 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
     if (track)
         for (uint32_t i = 0; i < x; i++) b[i] = checks[i] < N ? bc[checks[i]] : 0.0f;
     for (int s = 0; s < nb; s++) {
-        if (c > 0 && s > 0) {
+        if (c > 0 && off + s > 0) {
             bool sat = true;
             for (uint32_t i = 0; i < x && sat; i++) {
                 const float bv = track ? b[i] : 0.0f;
@@ -358,11 +372,12 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
             }
         }
         if (!track) continue;
-        const uint32_t r = bi->root[s];
+        const int l = lane0 + s;
+        const uint32_t r = bi->root[l];
         const uint32_t rr = reach[r];
-        const uint32_t all = (bi->H == 1 ? (uint32_t)bi->rsum[s] : 0u) + rr;
-        const unsigned long long nvt = bi->nvis[s] + all;
-        const double p = bi->p[s];
+        const uint32_t all = (bi->H == 1 ? (uint32_t)bi->rsum[l] : 0u) + rr;
+        const unsigned long long nvt = bi->nvis[l] + all;
+        const double p = bi->p[l];
         for (uint32_t i = 0; i < x; i++) {
             const uint32_t v = checks[i];
             if (v >= N) continue;
@@ -370,27 +385,30 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
                 if (rr > 0) b[i] = __fadd_rn(b[i], bc_root_term(rr, nvt));
                 continue;
             }
-            const float dv = ((seen[v] >> s) & 1u) ? mdelta[(uint64_t)v * AXBC_W + s]
+            const float dv = ((seen[v] >> l) & 1u) ? mdelta[(uint64_t)v * AXBC_W + l]
                                                    : __uint2float_rn(reach[v]);
             if (dv == 0.0f && p > 0.0) continue;
             b[i] = __fadd_rn(b[i], bc_term(dv, rr, p));
         }
     }
-    bi->napply = stop;
+    // lanes [lane0, lane0 + nb) of the pass: the first `stop` are applied
+    const uint32_t seg = (nb >= 32 ? FULL_MASK : ((1u << nb) - 1u)) << lane0;
+    const uint32_t app = (stop >= 32 ? FULL_MASK : ((1u << stop) - 1u)) << lane0;
+    bi->applymask = (bi->applymask & ~seg) | app;
     ss->napply = stop;
     for (int s = 0; s < stop; s++) {
         if (ss->nrounds < hist_cap) {
-            hist_v[ss->nrounds] = ss->v0[s];
-            hist_p[ss->nrounds] = ss->p[s];
+            hist_v[ss->nrounds] = ss->v0[off + s];
+            hist_p[ss->nrounds] = ss->p[off + s];
         }
         ss->nrounds++;
-        ss->skipped += ss->skip_before[s];
-        ss->te += 2 * bi->te[s];
+        ss->skipped += ss->skip_before[off + s];
+        ss->te += 2 * bi->te[lane0 + s];
     }
     if (stop < nb) {
         ss->stopped = 1;
         ss->done = 1;
-    } else {
+    } else if (last) {
         if (ss->skipped_run) {
             bool sat = false;
             if (c > 0 && nb > 0) {
@@ -443,8 +461,8 @@ extern "C" int axbc_run_sampled(axbc_ctx *c, const axbc_run_params *prm, axbc_ru
     const uint64_t n = g->n;
     CHECK_ARG(prm->z >= 0 && prm->z <= 6, "axbc_run_sampled: heuristic must be in [0,6]");
     CHECK_ARG(prm->H == 0 || prm->H == 1, "axbc_run_sampled: H must be 0 or 1");
-    CHECK_ARG(prm->batch_width >= 1 && prm->batch_width <= AXBC_MAX_BATCH,
-              "axbc_run_sampled: batch_width must be in [1, 32]");
+    CHECK_ARG(prm->batch_width >= 1 && prm->batch_width <= AXBC_MAX_WIDTH,
+              "axbc_run_sampled: batch_width must be in [1, 64]");
     CHECK_ARG(prm->nchecks <= n, "axbc_run_sampled: more check vertices than vertices");
     TRY(ensure_sampler(c, prm->nchecks));
     cudaStream_t s = c->stream;
@@ -514,24 +532,38 @@ extern "C" int axbc_run_sampled(axbc_ctx *c, const axbc_run_params *prm, axbc_ru
         }
         {
             ProfScope ps(c, KP_SAMPLER, 0);
-            k_sampler<<<1, 1, 0, s>>>(c->ss, D, c->used, c->checks, c->bi, g->S_lcc);
+            k_sampler<<<1, 1, 0, s>>>(c->ss, D, c->used, c->checks, g->S_lcc);
         }
         CU_LAUNCH("k_sampler");
         CU(cudaMemcpyAsync(c->ss_host, c->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
         const int nb = c->ss_host->nb;
         if (c->ss_host->done && nb == 0 && c->ss_host->skipped_run == 0) break;
-        if (nb > 0) {
-            TRY(axbc_batch_traverse(c, nb, prm->H));
-            batches++;
+        // the round's pivots in passes of at most AXBC_W lanes; the Bader
+        // replay of each pass sees the bc of the passes before it
+        for (int off = 0; off == 0 || off < nb; off += AXBC_W) {
+            const int cnt = std::min(nb - off, AXBC_W);
+            if (cnt > 0) {
+                k_load_pass<<<1, AXBC_W, 0, s>>>(c->ss, c->bi, off, 0);
+                CU_LAUNCH("k_load_pass");
+                TRY(axbc_batch_traverse(c, cnt, prm->H));
+                batches++;
+            }
+            {
+                ProfScope ps(c, KP_SAMPLER, 0);
+                k_sampler_post<<<1, 1, 0, s>>>(c->ss, c->bi, c->bc, c->mdelta, c->seen, g->reach,
+                                               c->checks, c->checkval, hist_v, hist_p, nbfs + 1, off, 0);
+            }
+            CU_LAUNCH("k_sampler_post");
+            if (cnt > 0) TRY(axbc_batch_apply(c));
+            if (off + AXBC_W < nb) {
+                // a later pass runs only if Bader's test did not stop the round
+                CU(cudaMemcpyAsync(&c->ss_host->done, &c->ss->done, sizeof(int32_t),
+                                   cudaMemcpyDeviceToHost, s));
+                CU(cudaStreamSynchronize(s));
+                if (c->ss_host->done) break;
+            }
         }
-        {
-            ProfScope ps(c, KP_SAMPLER, 0);
-            k_sampler_post<<<1, 1, 0, s>>>(c->ss, c->bi, c->bc, c->mdelta, c->seen, g->reach,
-                                           c->checks, c->checkval, hist_v, hist_p, nbfs + 1);
-        }
-        CU_LAUNCH("k_sampler_post");
-        if (nb > 0) TRY(axbc_batch_apply(c));
     }
     CU(cudaMemcpyAsync(c->ss_host, c->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));

@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no e2e pass")
     ap.add_argument("--skip-plain", action="store_true", help="profiling runs: no plain pass")
+    ap.add_argument("--push-factor", type=float, default=None,
+                    help="fixed batched push/pull factor instead of autotuning (profiling runs)")
     return ap.parse_args()
 
 
@@ -196,7 +198,13 @@ def main():
     deg = G.deg()
     rng = np.random.default_rng(1234)
     trial = rng.choice(np.flatnonzero(deg > 0), size=32, replace=False).astype(np.uint32)
-    tuning = ctx.autotune(trial) if args.impl == "gb300" else None
+    tuning = None
+    if args.impl == "gb300" and args.push_factor is not None:
+        ctx.set_tuning(32.0, args.push_factor)
+        tuning = {"push_factor_single": 32.0, "push_factor_batch": args.push_factor,
+                  "batch_width": args.width, "fixed": True}
+    elif args.impl == "gb300":
+        tuning = ctx.autotune(trial)
     if tuning:
         config["tuning"] = {k: (round(v, 4) if isinstance(v, float) else v)
                             for k, v in tuning.items() if "factor" in k or k == "batch_width"}

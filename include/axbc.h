@@ -37,6 +37,9 @@ enum {
 
 /* Batch width of the multi-source pass (sources per warp bitmask). */
 #define AXBC_MAX_BATCH 32
+/* largest sampling width of a sampled run: a round draws up to 64 pivots from
+ * one snapshot and traverses them as passes of at most AXBC_MAX_BATCH */
+#define AXBC_MAX_WIDTH 64
 
 typedef struct axbc_graph axbc_graph;
 typedef struct axbc_ctx axbc_ctx;
@@ -180,7 +183,7 @@ typedef struct {
     uint32_t nchecks;     /* check vertices */
     int32_t H;            /* 1: one-degree reach terms */
     int64_t seed;         /* srand48 seed; 4343543 is the reference default */
-    int32_t batch_width;  /* 1..AXBC_MAX_BATCH */
+    int32_t batch_width;  /* 1..AXBC_MAX_WIDTH pivots drawn per snapshot */
     int32_t pad;
 } axbc_run_params;
 

@@ -1,6 +1,6 @@
 """The benchmark configurations as parity cases at full size.
 
-Config 2: Kronecker scale 20, one-degree reduction (-H 1), heuristic 1.
+Config 2: Kronecker scale 20, one-degree reduction (-H 1), heuristic 1, width 64.
 Config 3: 2048x2048 grid, 2% of edges dropped (seed 7), 0.01% long-range edges,
 heuristic 4 with Bader's stop (-c 1 -x 8).  On this graph uint32 path counts
 wrap and floats overflow (hundreds of BFS levels): comparisons are type for
@@ -36,8 +36,8 @@ def test_config2_scale20_H1_z1_sampled(axbc, orc, kron20):
     G, g = kron20
     assert int(g.reach.sum()) > 0  # leaves were folded into reach
     ctx = axbc.Context(G)
-    got = ctx.run_sampled(z=1, nbfs=40, bader_c=0, nchecks=1, H=1, seed=1, W=32)
-    want = orc.run(g, z=1, nbfs=40, bader_c=0, nchecks=1, H=1, seed=1, W=32)
+    got = ctx.run_sampled(z=1, nbfs=80, bader_c=0, nchecks=1, H=1, seed=1, W=64)
+    want = orc.run(g, z=1, nbfs=80, bader_c=0, nchecks=1, H=1, seed=1, W=64)
     assert np.array_equal(got["pivots"], want["pivots"])
     assert np.array_equal(got["probs"], want["probs"])
     assert got["te"] == want["te"] and got["skipped"] == want["skipped"]
@@ -47,9 +47,9 @@ def test_config2_scale20_H1_z1_sampled(axbc, orc, kron20):
 def test_config2_full_budget_runs_and_is_deterministic(axbc, kron20):
     G, _ = kron20
     ctx = axbc.Context(G)
-    a = ctx.run_sampled(z=1, nbfs=4096, bader_c=0, nchecks=1, H=1, seed=1, W=32)
+    a = ctx.run_sampled(z=1, nbfs=4096, bader_c=0, nchecks=1, H=1, seed=1, W=64)
     bc_a = ctx.bc()
-    b = ctx.run_sampled(z=1, nbfs=4096, bader_c=0, nchecks=1, H=1, seed=1, W=32)
+    b = ctx.run_sampled(z=1, nbfs=4096, bader_c=0, nchecks=1, H=1, seed=1, W=64)
     assert a["nrounds"] == b["nrounds"] and a["te"] == b["te"] and a["nrounds"] > 1000
     assert np.array_equal(bc_a, ctx.bc())
     assert np.all(bc_a >= 0)

@@ -141,9 +141,10 @@ def test_heavy_vertices_and_directed(axbc, orc, undirected):
         assert_float_exact(ctx.bc(), want6, f"plain bc, push factor {factor}")
 
 
-@pytest.mark.parametrize("W", [1, 32])
+@pytest.mark.parametrize("W", [1, 32, 64])
 @pytest.mark.parametrize("z", [0, 1, 2, 3, 4, 5, 6])
 def test_sampled_run_matches_oracle(axbc, orc, z, W):
+    """W = 64 draws 64 pivots per snapshot and traverses them as two passes."""
     H = 1 if z in (1, 3) else 0
     g, G = make(axbc, orc, golden_edges(), 1024, True, H)
     ctx = axbc.Context(G)
@@ -159,7 +160,7 @@ def test_sampled_run_matches_oracle(axbc, orc, z, W):
     assert_float_exact(ctx.delta(), want["delta_last"], "last delta")
 
 
-@pytest.mark.parametrize("W", [1, 8, 32])
+@pytest.mark.parametrize("W", [1, 8, 32, 40, 64])
 def test_bader_stop_matches_oracle(axbc, orc, W):
     g, G = make(axbc, orc, golden_edges(), 1024)
     ctx = axbc.Context(G)
