@@ -49,6 +49,21 @@ class RunResult(C.Structure):
                 ("batches", C.c_int32)]
 
 
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("result", RunResult),
+                ("bytes", C.c_uint64), ("submit_ns", C.c_uint64), ("start_ns", C.c_uint64),
+                ("finish_ns", C.c_uint64), ("error", C.c_char * 256)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("budget", C.c_uint64), ("in_use", C.c_uint64), ("queued", C.c_uint64),
+                ("admitted", C.c_uint64), ("completed", C.c_uint64), ("passes", C.c_uint64),
+                ("lanes", C.c_uint64)]
+
+
+REQ_STATES = ["queued", "running", "done", "failed"]
+
+
 # name -> (restype, argtypes) of every entry point this binding uses
 _P = C.c_void_p
 _U32P = C.POINTER(C.c_uint32)
@@ -100,6 +115,20 @@ _SIGS = {
                                        C.c_double, C.c_int, _P, _P, C.POINTER(PivotStats)]),
     "axbc_selftest_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_uint64)]),
+    "axbc_srand48": (C.c_uint64, [C.c_int64]),
+    "axbc_sample": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int,
+                              C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
+    "axbc_bader_check": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(C.c_int)]),
+    "axbc_server_create": (C.c_int, [C.c_uint64, C.POINTER(_P)]),
+    "axbc_server_add_graph": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
+    "axbc_request_submit": (C.c_int, [_P, C.c_int, C.POINTER(RunParams), C.POINTER(C.c_uint64)]),
+    "axbc_request_poll": (C.c_int, [_P, C.c_uint64, C.POINTER(RequestInfo)]),
+    "axbc_request_wait": (C.c_int, [_P, C.c_uint64, C.c_int64, C.POINTER(RequestInfo)]),
+    "axbc_request_result": (C.c_int, [_P, C.c_uint64, _P, _P, _P, C.c_uint64,
+                                      C.POINTER(C.c_uint64)]),
+    "axbc_request_release": (C.c_int, [_P, C.c_uint64]),
+    "axbc_server_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "axbc_server_destroy": (C.c_int, [_P]),
 }
 
 PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bwd",
@@ -340,6 +369,22 @@ class Context:
                     push_factor_batch=t.push_factor_batch, batch_width=t.batch_width,
                     batch_te_per_s=t.batch_te_per_s, plain_te_per_s=t.plain_te_per_s)
 
+    def sample(self, z, rng, mix=0, first=False):
+        """One draw of heuristic z from this context's bc / last delta:
+        (v0, p, rng', mix') -- rng is a drand48 state (see srand48)."""
+        r, m = C.c_uint64(rng), C.c_uint32(mix)
+        v, p = C.c_uint32(), C.c_double()
+        _check(lib().axbc_sample(self._h, z, C.byref(r), C.byref(m), int(first), C.byref(v),
+                                 C.byref(p)))
+        return v.value, p.value, r.value, m.value
+
+    def bader_check(self, checks, c):
+        """True if every check vertex v has bc[v] / 2 >= c * n."""
+        ch = np.ascontiguousarray(checks, dtype=np.uint32)
+        out = C.c_int()
+        _check(lib().axbc_bader_check(self._h, _ptr(ch), len(ch), c, C.byref(out)))
+        return bool(out.value)
+
     def profile(self, enable=True):
         """Record CUDA events around every kernel launch of this context."""
         _check(lib().axbc_ctx_profile(self._h, int(enable)))
@@ -362,6 +407,86 @@ class Context:
     def close(self):
         if getattr(self, "_h", None):
             lib().axbc_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def srand48(seed):
+    """The drand48 state that srand48(seed) sets."""
+    return lib().axbc_srand48(seed)
+
+
+class Server:
+    """Request server over resident graphs (axbc_server_* / axbc_request_*).
+
+    Requests are sampled runs (run_sampled's parameters, W <= 32); the server
+    batches the rounds of concurrent requests on one graph into shared passes.
+    """
+
+    def __init__(self, hbm_budget=0):
+        h = _P()
+        _check(lib().axbc_server_create(int(hbm_budget), C.byref(h)))
+        self._h = h
+        self._graphs = []
+
+    def add_graph(self, graph, H=0):
+        gid = C.c_int()
+        _check(lib().axbc_server_add_graph(self._h, graph._h, H, C.byref(gid)))
+        self._graphs.append(graph)  # keeps the graph alive as long as the server
+        return gid.value
+
+    def submit(self, graph_id, z=0, nbfs=1, bader_c=0, nchecks=1, H=0, seed=4343543, W=1):
+        prm = RunParams(z, bader_c, nbfs, nchecks, H, seed, W, 0)
+        rid = C.c_uint64()
+        _check(lib().axbc_request_submit(self._h, graph_id, C.byref(prm), C.byref(rid)))
+        return rid.value
+
+    @staticmethod
+    def _info(i):
+        r = i.result
+        return dict(state=REQ_STATES[i.state], status=i.status, bytes=i.bytes,
+                    submit_ns=i.submit_ns, start_ns=i.start_ns, finish_ns=i.finish_ns,
+                    error=i.error.decode(), nrounds=r.nrounds, skipped=r.skipped,
+                    dropped=r.dropped, ui_end=r.rounds, te=r.te, stopped=bool(r.stopped),
+                    batches=r.batches)
+
+    def poll(self, rid):
+        i = RequestInfo()
+        _check(lib().axbc_request_poll(self._h, rid, C.byref(i)))
+        return self._info(i)
+
+    def wait(self, rid, timeout_ms=-1):
+        i = RequestInfo()
+        _check(lib().axbc_request_wait(self._h, rid, int(timeout_ms), C.byref(i)))
+        return self._info(i)
+
+    def result(self, rid, n):
+        """(bc, pivots, probs) of a done request on an n-vertex graph."""
+        cnt = C.c_uint64()
+        _check(lib().axbc_request_result(self._h, rid, None, None, None, 0, C.byref(cnt)))
+        bc = np.zeros(n, np.float32)
+        piv = np.zeros(cnt.value, np.uint32)
+        pr = np.zeros(cnt.value, np.float64)
+        _check(lib().axbc_request_result(self._h, rid, _ptr(bc), _ptr(piv), _ptr(pr), cnt.value,
+                                         C.byref(cnt)))
+        return bc, piv, pr
+
+    def release(self, rid):
+        _check(lib().axbc_request_release(self._h, rid))
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().axbc_server_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().axbc_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -24,7 +24,7 @@ CLI = os.path.join(HERE, "axbc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-Xcompiler", "-Wno-unused-function", "-I", os.path.join(ROOT, "include")]
-LIB_SOURCES = ["api.cu", "graph.cu", "single.cu", "batch.cu", "sampler.cu", "compat.cu",
+LIB_SOURCES = ["api.cu", "graph.cu", "single.cu", "batch.cu", "sampler.cu", "serve.cu", "compat.cu",
                "tune.cu", "noalloc.cu", "host_graph.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 

@@ -18,7 +18,7 @@ static __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * AXB
 
 // resident blocks per SM the pull kernel is compiled for (its register budget)
 #ifndef AXBC_PULL_MIN_BLOCKS
-#define AXBC_PULL_MIN_BLOCKS 6
+#define AXBC_PULL_MIN_BLOCKS 8
 #endif
 
 // Per-level vertex lists: the vertices whose level-L mask is nonzero, appended
@@ -155,6 +155,15 @@ __device__ __forceinline__ void list_append(const LevelLists &ll, int L, bool is
     if (isnew && idx < ll.cap[L]) ll.pool[ll.start[L] + idx] = v;
 }
 
+// List entries per work unit: 32, or fewer when the list is too short to give
+// every resident warp a unit (a short list of high-degree vertices would
+// otherwise sit on a few warps).
+__device__ __forceinline__ uint32_t list_unit(uint32_t lcnt)
+{
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    return max(1u, min(32u, lcnt / nwarps));
+}
+
 // the stored list of level L, or nullptr when the level overflowed its capacity
 __device__ __forceinline__ const uint32_t *level_list(const LevelLists &ll, int L, uint32_t &cnt)
 {
@@ -261,7 +270,8 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
     const uint64_t nhi = a.n_heavy_items;
     uint32_t lcnt = 0;
     const uint32_t *lst = level_list(ll, L - 1, lcnt);  // the frontier, when stored
-    const uint64_t nu = lst ? nhi + (lcnt + 31) / 32 : n_units(a);
+    const uint32_t ent = list_unit(lcnt);
+    const uint64_t nu = lst ? nhi + (lcnt + ent - 1) / ent : n_units(a);
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -274,9 +284,9 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
             continue;
         }
         if (lst) {
-            const uint32_t i = (uint32_t)(t - nhi) * 32 + lane;
+            const uint32_t i = (uint32_t)(t - nhi) * ent + lane;
             uint32_t v_l = 0, f_l = 0;
-            if (i < lcnt) {
+            if (lane < ent && i < lcnt) {
                 v_l = lst[i];
                 if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fprev[v_l];
             }
@@ -740,7 +750,8 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
 {
     const unsigned lane = lane_id();
     const uint64_t nhi = a.n_heavy_items;
-    const uint64_t nu = lst ? nhi + (lcnt + 31) / 32 : n_units(a);
+    const uint32_t ent = list_unit(lcnt);
+    const uint64_t nu = lst ? nhi + (lcnt + ent - 1) / ent : n_units(a);
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -758,9 +769,9 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
             continue;
         }
         if (lst) {
-            const uint32_t i = (uint32_t)(t - nhi) * 32 + lane;
+            const uint32_t i = (uint32_t)(t - nhi) * ent + lane;
             uint32_t v_l = 0, f_l = 0;
-            if (i < lcnt) {
+            if (lane < ent && i < lcnt) {
                 v_l = lst[i];
                 if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fd[v_l] & dmask;
             }
@@ -883,6 +894,10 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
     __shared__ unsigned long long s_nvt[AXBC_W];
     __shared__ InvSplit s_iv[AXBC_W];
     __shared__ float *s_bc[AXBC_W];
+    // per lane: float(reach_v0 + 1), the split 1/p, and whether the fast
+    // division applies (bit 0) and zero terms may be skipped (bit 1)
+    __shared__ float4 s_k[AXBC_W];
+    __shared__ int s_single;  // every applied lane updates the same vector
     // per warp, two chunks: the dependency rows of 32 vertices, padded to 33
     // floats so that thread t reading row t, column s hits bank (t + s) mod 32
     __shared__ float s_rows[UPD_TPB / 32][2][32][33];
@@ -908,9 +923,23 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
             s_nvt[s] = 2;
             s_iv[s] = inv_split(1.0);
         }
+        const InvSplit iv = s_iv[s];
+        s_k[s] = make_float4(__uint2float_rn(s_reach[s] + 1u), iv.hi, iv.lo,
+                             __uint_as_float((iv.ok ? 1u : 0u) | (s_skip0[s] ? 2u : 0u)));
+        if (s == 0) {
+            int single = 1;
+            float *t0 = nullptr;
+            for (int l = 0; l < AXBC_W; l++)
+                if ((amask >> l) & 1u) {
+                    if (!t0) t0 = bi->lane_bc[l];
+                    else if (bi->lane_bc[l] != t0) single = 0;
+                }
+            s_single = single;
+        }
     }
     __syncthreads();
     if (amask == 0) return;
+    const bool single = s_single != 0;
     const int slast = 31 - __clz(amask);
     const unsigned lane = lane_id();
     const unsigned wid = threadIdx.x >> 5;
@@ -941,7 +970,27 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         const uint64_t v = base + lane;
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
-        if (sv != 0u || rv != 0u) {
+        if ((sv != 0u || rv != 0u) && single) {
+            // one target vector: all 32 lanes unrolled, lane order kept
+            const float(*rows)[33] = s_rows[wid][buf];
+            const float rf = __uint2float_rn(rv);
+            float *tgt = s_bc[slast];
+            float b = tgt[v];
+#pragma unroll
+            for (int s = 0; s < AXBC_W; s++) {
+                if (!((amask >> s) & 1u)) continue;
+                if ((uint32_t)v == s_root[s]) {
+                    if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
+                    continue;
+                }
+                const float dv = ((sv >> s) & 1u) ? rows[lane][s] : rf;
+                const float4 k = s_k[s];
+                const uint32_t fl = __float_as_uint(k.w);
+                if (dv == 0.0f && (fl & 2u)) continue;
+                b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
+            }
+            tgt[v] = b;
+        } else if (sv != 0u || rv != 0u) {
             const float(*rows)[33] = s_rows[wid][buf];
             const float rf = __uint2float_rn(rv);
             // lanes in order; consecutive lanes of one run add into one

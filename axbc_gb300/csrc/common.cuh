@@ -337,12 +337,12 @@ __host__ __device__ __forceinline__ InvSplit inv_split(double p)
     r.ok = 1;
     return r;
 }
-__device__ __forceinline__ float div_to_float(float x, double p, InvSplit iv)
+__device__ __forceinline__ float div_to_float_hl(float x, double p, float hi, float lo, bool ok)
 {
-    if (iv.ok && x > 0.0f && x < 3.0e38f) {
-        const float a = __fmul_rn(x, iv.hi);
-        const float e = __fmaf_rn(x, iv.hi, -a);
-        const float b = __fmaf_rn(x, iv.lo, e);
+    if (ok && x > 0.0f && x < 3.0e38f) {
+        const float a = __fmul_rn(x, hi);
+        const float e = __fmaf_rn(x, hi, -a);
+        const float b = __fmaf_rn(x, lo, e);
         const float s = __fadd_rn(a, b);
         const float bb = __fsub_rn(s, a);
         const float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
@@ -358,6 +358,10 @@ __device__ __forceinline__ float div_to_float(float x, double p, InvSplit iv)
         }
     }
     return __double2float_rn(__ddiv_rn((double)x, p));
+}
+__device__ __forceinline__ float div_to_float(float x, double p, InvSplit iv)
+{
+    return div_to_float_hl(x, p, iv.hi, iv.lo, iv.ok != 0);
 }
 __device__ __forceinline__ float bc_term_fast(float delta_v, uint32_t reach_v0, double p, InvSplit iv)
 {

@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "sampled.cuh"
 
 struct SamplerState {
     uint64_t rng;
@@ -197,6 +198,78 @@ __global__ void k_sampler_init(SamplerState *ss, uint32_t *checks, int64_t seed,
     ss->skipped_run = 0;
 }
 
+// One draw of heuristic z (dist_mix: the -z 6 mixture state): v0 and its
+// probability, the reference's rules of src/axbc2d.c:2873-3051.  snap0: no
+// pivot applied yet (the dynamic heuristics then draw uniformly).
+__device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, const SamplerDists &D,
+                           bool snap0, double S_bc, double S_d, double S_lcc, uint32_t &v0,
+                           double &prob)
+{
+    int found;
+    prob = 0;
+    if (dist_mix == 0 || z == 0) {
+        v0 = d_uniform_int(x, (uint32_t)N, 0);
+        prob = __ddiv_rn(1.0, (double)N);
+    } else if (dist_mix == 1 || z == 1) {
+        // high-degree neighbourhood (src/axbc2d.c:2890-2917)
+        const uint32_t r = d_uniform_int(x, D.sum_deg, 0);
+        uint64_t h = d_find_u32(D.deg2p, D.seg_end, D.n_seg, r, &found);
+        if (!found) h = N - 1;
+        const uint32_t dh = D.col[h + 1] - D.col[h];
+        if (dh > 0) {
+            uint32_t k = 0;
+            if (dh != 1) k = d_uniform_int(x, dh - 1, 0);
+            h = D.row[D.col[h] + k];
+        }
+        v0 = (uint32_t)h;
+        prob = __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg);
+    } else if (dist_mix == 2 || z == 2) {
+        // LCC (src/axbc2d.c:2919-2937)
+        const double r = __dmul_rn(d_uniform01(x), S_lcc);
+        uint64_t h = d_hsearch(D.lcc_local, D.lcc_csum, N, r, &found);
+        if (!found) h = N - 1;
+        v0 = (uint32_t)h;
+        prob = __ddiv_rn((double)D.lcc[v0], S_lcc);
+    } else if (dist_mix == 3 || z == 3 || dist_mix == 4 || z == 4 || dist_mix == 5 || z == 5) {
+        const int kind = (dist_mix == 3 || z == 3) ? 3 : (dist_mix == 4 || z == 4) ? 4 : 5;
+        if (snap0) {
+            v0 = d_uniform_int(x, (uint32_t)N, 0);
+            prob = __ddiv_rn(1.0, (double)N);
+        } else if (kind == 4) {
+            // delta of the last pivot (src/axbc2d.c:2970-2991)
+            const double r = __dmul_rn(d_uniform01(x), S_d);
+            uint64_t h = d_hsearch(D.d_local, D.d_csum, N, r, &found);
+            if (!found) h = N - 1;
+            v0 = (uint32_t)h;
+            prob = __ddiv_rn((double)D.delta_last[v0], S_d);
+        } else {
+            // bc (src/axbc2d.c:2941-2969) or 1/(1+bc) (2995-3022)
+            const double r = __dmul_rn(d_uniform01(x), S_bc);
+            uint64_t h = d_hsearch(D.bc_local, D.bc_csum, N, r, &found);
+            if (!found) h = N - 1;
+            v0 = (uint32_t)h;
+            if (kind == 3) prob = __ddiv_rn((double)D.bc[v0], S_bc);
+            else prob = __ddiv_rn(__ddiv_rn(1.0, __dadd_rn((double)D.bc[v0], 1.0)), S_bc);
+        }
+    }
+    if (z == 6) {
+        // mixture probability (src/axbc2d.c:3026-3051)
+        prob = __ddiv_rn(1.0, (double)N);
+        if (snap0) {
+            prob = __dadd_rn(prob, __ddiv_rn(1.0, (double)N));
+            prob = __dadd_rn(prob, __ddiv_rn(1.0, (double)N));
+        } else if (v0 < N) {
+            prob = __dadd_rn(prob, __ddiv_rn((double)D.bc[v0], S_bc));
+            prob = __dadd_rn(prob, __ddiv_rn((double)D.delta_last[v0], S_d));
+        }
+        if (v0 < N) {
+            prob = __dadd_rn(prob, __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg));
+            prob = __dadd_rn(prob, __ddiv_rn((double)D.lcc[v0], S_lcc));
+            prob = __ddiv_rn(prob, 5.0);
+        }
+        dist_mix = d_uniform_int(x, 2, 0);
+    }
+}
 // Draw the rounds of one batch: up to W accepted pivots.
 __global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const uint32_t *checks,
                           double S_lcc)
@@ -230,71 +303,8 @@ __global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const
         uint32_t BSM = 0;
         bool good = false;
         while (!good) {
-            int found;
             if (BSM > LIM) break;
-            prob = 0;
-            if (dist_mix == 0 || z == 0) {
-                v0 = d_uniform_int(x, (uint32_t)N, 0);
-                prob = __ddiv_rn(1.0, (double)N);
-            } else if (dist_mix == 1 || z == 1) {
-                // high-degree neighbourhood (src/axbc2d.c:2890-2917)
-                const uint32_t r = d_uniform_int(x, D.sum_deg, 0);
-                uint64_t h = d_find_u32(D.deg2p, D.seg_end, D.n_seg, r, &found);
-                if (!found) h = N - 1;
-                const uint32_t dh = D.col[h + 1] - D.col[h];
-                if (dh > 0) {
-                    uint32_t k = 0;
-                    if (dh != 1) k = d_uniform_int(x, dh - 1, 0);
-                    h = D.row[D.col[h] + k];
-                }
-                v0 = (uint32_t)h;
-                prob = __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg);
-            } else if (dist_mix == 2 || z == 2) {
-                // LCC (src/axbc2d.c:2919-2937)
-                const double r = __dmul_rn(d_uniform01(x), S_lcc);
-                uint64_t h = d_hsearch(D.lcc_local, D.lcc_csum, N, r, &found);
-                if (!found) h = N - 1;
-                v0 = (uint32_t)h;
-                prob = __ddiv_rn((double)D.lcc[v0], S_lcc);
-            } else if (dist_mix == 3 || z == 3 || dist_mix == 4 || z == 4 || dist_mix == 5 || z == 5) {
-                const int kind = (dist_mix == 3 || z == 3) ? 3 : (dist_mix == 4 || z == 4) ? 4 : 5;
-                if (snap0) {
-                    v0 = d_uniform_int(x, (uint32_t)N, 0);
-                    prob = __ddiv_rn(1.0, (double)N);
-                } else if (kind == 4) {
-                    // delta of the last pivot (src/axbc2d.c:2970-2991)
-                    const double r = __dmul_rn(d_uniform01(x), S_d);
-                    uint64_t h = d_hsearch(D.d_local, D.d_csum, N, r, &found);
-                    if (!found) h = N - 1;
-                    v0 = (uint32_t)h;
-                    prob = __ddiv_rn((double)D.delta_last[v0], S_d);
-                } else {
-                    // bc (src/axbc2d.c:2941-2969) or 1/(1+bc) (2995-3022)
-                    const double r = __dmul_rn(d_uniform01(x), S_bc);
-                    uint64_t h = d_hsearch(D.bc_local, D.bc_csum, N, r, &found);
-                    if (!found) h = N - 1;
-                    v0 = (uint32_t)h;
-                    if (kind == 3) prob = __ddiv_rn((double)D.bc[v0], S_bc);
-                    else prob = __ddiv_rn(__ddiv_rn(1.0, __dadd_rn((double)D.bc[v0], 1.0)), S_bc);
-                }
-            }
-            if (z == 6) {
-                // mixture probability (src/axbc2d.c:3026-3051)
-                prob = __ddiv_rn(1.0, (double)N);
-                if (snap0) {
-                    prob = __dadd_rn(prob, __ddiv_rn(1.0, (double)N));
-                    prob = __dadd_rn(prob, __ddiv_rn(1.0, (double)N));
-                } else if (v0 < N) {
-                    prob = __dadd_rn(prob, __ddiv_rn((double)D.bc[v0], S_bc));
-                    prob = __dadd_rn(prob, __ddiv_rn((double)D.delta_last[v0], S_d));
-                }
-                if (v0 < N) {
-                    prob = __dadd_rn(prob, __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg));
-                    prob = __dadd_rn(prob, __ddiv_rn((double)D.lcc[v0], S_lcc));
-                    prob = __ddiv_rn(prob, 5.0);
-                }
-                dist_mix = d_uniform_int(x, 2, 0);
-            }
+            d_draw_one(x, dist_mix, z, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
             if (v0 < N && used[v0]) BSM++;
             else good = true;
         }
@@ -430,6 +440,242 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
     ss->nrounds_snap = ss->nrounds;
 }
 
+// ------------------------------------------------------------ sampled runs
+// Device state of one sampled run lives in a SampledRun (sampled.cuh): the
+// context's own buffers for axbc_run_sampled, or buffers of its own for a
+// request of the server.
+
+uint64_t sr_bytes(uint64_t n, const axbc_run_params *prm)
+{
+    const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    const uint64_t nbfs = prm->nbfs < n ? prm->nbfs : n;
+    uint64_t b = sizeof(SamplerState) + n * 4 * 2 + n + (prm->nchecks + 1) * 8 + (nbfs + 1) * 12;
+    const int z = prm->z;
+    if (z == 3 || z == 5 || z == 6) b += n * 8 + nb * 8;
+    if (z == 4 || z == 6) b += n * 8 + nb * 8;
+    return b;
+}
+
+static void sr_release(SampledRun *r, bool own)
+{
+    if (own) {
+        axbc_dfree(r->ss);
+        if (r->ss_host) cudaFreeHost(r->ss_host);
+        axbc_dfree(r->bc);
+        axbc_dfree(r->delta_last);
+        axbc_dfree(r->used);
+        axbc_dfree(r->checks);
+        axbc_dfree(r->checkval);
+        axbc_dfree(r->dyn_local);
+        axbc_dfree(r->dyn_csum);
+        axbc_dfree(r->dyn_local2);
+        axbc_dfree(r->dyn_csum2);
+    }
+    axbc_dfree(r->hist_v);
+    axbc_dfree(r->hist_p);
+    r->hist_v = nullptr;
+    r->hist_p = nullptr;
+}
+
+void sr_free(SampledRun *r) { sr_release(r, true); }
+
+static int sr_alloc_hist(SampledRun *r, uint64_t n)
+{
+    const uint64_t nbfs = r->prm.nbfs < n ? r->prm.nbfs : n;
+    r->hist_cap = nbfs + 1;
+    TRY(axbc_dalloc((void **)&r->hist_v, r->hist_cap * 4, nullptr));
+    TRY(axbc_dalloc((void **)&r->hist_p, r->hist_cap * 8, nullptr));
+    return AXBC_OK;
+}
+
+int sr_alloc(axbc_graph *g, const axbc_run_params *prm, SampledRun *r)
+{
+    const uint64_t n = g->n;
+    memset(r, 0, sizeof(*r));
+    r->prm = *prm;
+    const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    int st = AXBC_OK;
+#define SR_TRY(x)                   \
+    do {                            \
+        if ((st = (x)) != AXBC_OK) { \
+            sr_release(r, true);    \
+            return st;              \
+        }                           \
+    } while (0)
+    SR_TRY(axbc_dalloc((void **)&r->ss, sizeof(SamplerState), nullptr));
+    if (cudaMallocHost((void **)&r->ss_host, sizeof(SamplerState)) != cudaSuccess) {
+        sr_release(r, true);
+        axbc_set_error("sampled run: pinned host allocation failed");
+        return AXBC_ERR_NOMEM;
+    }
+    SR_TRY(axbc_dalloc((void **)&r->bc, n * 4, nullptr));
+    SR_TRY(axbc_dalloc((void **)&r->delta_last, n * 4, nullptr));
+    SR_TRY(axbc_dalloc((void **)&r->used, n, nullptr));
+    SR_TRY(axbc_dalloc((void **)&r->checks, (prm->nchecks + 1) * 4, nullptr));
+    SR_TRY(axbc_dalloc((void **)&r->checkval, (prm->nchecks + 1) * 4, nullptr));
+    const int z = prm->z;
+    if (z == 3 || z == 5 || z == 6) {
+        SR_TRY(axbc_dalloc((void **)&r->dyn_local, n * 8, nullptr));
+        SR_TRY(axbc_dalloc((void **)&r->dyn_csum, nb * 8, nullptr));
+    }
+    if (z == 4 || z == 6) {
+        SR_TRY(axbc_dalloc((void **)&r->dyn_local2, n * 8, nullptr));
+        SR_TRY(axbc_dalloc((void **)&r->dyn_csum2, nb * 8, nullptr));
+    }
+    SR_TRY(sr_alloc_hist(r, n));
+#undef SR_TRY
+    return AXBC_OK;
+}
+
+int sr_check_params(const axbc_graph *g, const axbc_run_params *prm, int max_width)
+{
+    CHECK_ARG(prm->z >= 0 && prm->z <= 6, "sampled run: heuristic must be in [0,6]");
+    CHECK_ARG(prm->H == 0 || prm->H == 1, "sampled run: H must be 0 or 1");
+    CHECK_ARG(prm->batch_width >= 1 && prm->batch_width <= max_width,
+              max_width == AXBC_W ? "sampled run: batch_width must be in [1, 32]"
+                                  : "sampled run: batch_width must be in [1, 64]");
+    CHECK_ARG(prm->nchecks <= g->n, "sampled run: more check vertices than vertices");
+    return AXBC_OK;
+}
+
+// reset the run's vectors and draw its check vertices (on the context's stream)
+int sr_begin(axbc_ctx *c, SampledRun *r)
+{
+    axbc_graph *g = c->g;
+    const uint64_t n = g->n;
+    cudaStream_t s = c->stream;
+    const int z = r->prm.z;
+    if (z == 1 || z == 6) TRY(axbc_build_deg_dist(g, s));
+    if (z == 2 || z == 6) TRY(axbc_build_lcc(g, s));
+    CU(cudaMemsetAsync(r->bc, 0, n * 4, s));
+    CU(cudaMemsetAsync(r->delta_last, 0, n * 4, s));
+    CU(cudaMemsetAsync(r->used, 0, n, s));
+    {
+        ProfScope ps(c, KP_SAMPLER, 0);
+        k_sampler_init<<<1, 1, 0, s>>>(r->ss, r->checks, r->prm.seed, z, r->prm.nbfs, n,
+                                       (uint32_t)r->prm.bader_c, r->prm.nchecks, r->prm.batch_width);
+    }
+    CU_LAUNCH("k_sampler_init");
+    r->batches = 0;
+    return AXBC_OK;
+}
+
+// draw the run's next round from its current bc / last delta; the sampler
+// state is copied to the pinned mirror (read it after the stream syncs)
+int sr_draw(axbc_ctx *c, SampledRun *r)
+{
+    axbc_graph *g = c->g;
+    const uint64_t n = g->n;
+    cudaStream_t s = c->stream;
+    const int z = r->prm.z;
+    SamplerDists D;
+    memset(&D, 0, sizeof(D));
+    D.col = g->fwd.col;
+    D.row = g->fwd.row;
+    D.deg2p = g->deg2p;
+    D.seg_end = g->seg_end;
+    D.sdn = g->sdn;
+    D.n_seg = g->n_seg;
+    D.sum_deg = g->sum_deg;
+    D.lcc = g->lcc;
+    D.lcc_local = g->lcc_local;
+    D.lcc_csum = g->lcc_csum;
+    D.bc = r->bc;
+    D.delta_last = r->delta_last;
+    const bool dyn_bc = z == 3 || z == 5 || z == 6;
+    const bool dyn_d = z == 4 || z == 6;
+    const uint64_t nbB = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    const unsigned hb = (unsigned)((nbB + 127) / 128);
+    if (dyn_bc) {
+        D.bc_local = r->dyn_local;
+        D.bc_csum = r->dyn_csum;
+        {
+            ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
+            k_hprefix_local<<<hb, 128, 0, s>>>(r->bc, n, r->dyn_local, r->dyn_csum, z == 5 ? 1 : 0, r->ss);
+        }
+        {
+            ProfScope ps(c, KP_SAMPLER, 0);
+            k_hprefix_csum<<<1, 1, 0, s>>>(r->dyn_csum, nbB, r->ss);
+        }
+    }
+    if (dyn_d) {
+        D.d_local = r->dyn_local2;
+        D.d_csum = r->dyn_csum2;
+        {
+            ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
+            k_hprefix_local<<<hb, 128, 0, s>>>(r->delta_last, n, r->dyn_local2, r->dyn_csum2, 0, r->ss);
+        }
+        {
+            ProfScope ps(c, KP_SAMPLER, 0);
+            k_hprefix_csum<<<1, 1, 0, s>>>(r->dyn_csum2, nbB, r->ss);
+        }
+    }
+    {
+        ProfScope ps(c, KP_SAMPLER, 0);
+        k_sampler<<<1, 1, 0, s>>>(r->ss, D, r->used, r->checks, g->S_lcc);
+    }
+    CU_LAUNCH("k_sampler");
+    CU(cudaMemcpyAsync(r->ss_host, r->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
+    return AXBC_OK;
+}
+
+int sr_nb(const SampledRun *r) { return r->ss_host->nb; }
+bool sr_finished(const SampledRun *r)
+{
+    return r->ss_host->done && r->ss_host->nb == 0 && r->ss_host->skipped_run == 0;
+}
+
+int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0)
+{
+    k_load_pass<<<1, AXBC_W, 0, c->stream>>>(r->ss, c->bi, off, lane0);
+    CU_LAUNCH("k_load_pass");
+    return AXBC_OK;
+}
+
+int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0)
+{
+    {
+        ProfScope ps(c, KP_SAMPLER, 0);
+        k_sampler_post<<<1, 1, 0, c->stream>>>(r->ss, c->bi, r->bc, c->mdelta, c->seen, c->g->reach,
+                                               r->checks, r->checkval, r->hist_v, r->hist_p,
+                                               r->hist_cap, off, lane0);
+    }
+    CU_LAUNCH("k_sampler_post");
+    return AXBC_OK;
+}
+
+// final counters, pivot history and check vertices of a finished run
+int sr_result(axbc_ctx *c, SampledRun *r, axbc_run_result *res, std::vector<uint32_t> *piv,
+              std::vector<double> *probs, std::vector<uint32_t> *checks)
+{
+    CU(cudaMemcpyAsync(r->ss_host, r->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    const SamplerState &S = *r->ss_host;
+    res->nrounds = S.nrounds;
+    res->skipped = S.skipped;
+    res->dropped = S.dropped;
+    res->rounds = S.ui;
+    res->te = S.te;
+    res->stopped = S.stopped;
+    res->batches = r->batches;
+    const uint64_t k = std::min<uint64_t>(S.nrounds, r->hist_cap);
+    if (piv) {
+        piv->resize(k);
+        if (k) CU(cudaMemcpy(piv->data(), r->hist_v, k * 4, cudaMemcpyDeviceToHost));
+    }
+    if (probs) {
+        probs->resize(k);
+        if (k) CU(cudaMemcpy(probs->data(), r->hist_p, k * 8, cudaMemcpyDeviceToHost));
+    }
+    if (checks) {
+        checks->resize(r->prm.nchecks);
+        if (r->prm.nchecks)
+            CU(cudaMemcpy(checks->data(), r->checks, r->prm.nchecks * 4, cudaMemcpyDeviceToHost));
+    }
+    return AXBC_OK;
+}
+
+// the context's own sampler buffers, grown on demand
 static int ensure_sampler(axbc_ctx *c, uint32_t nchecks)
 {
     const uint64_t n = c->g->n;
@@ -454,38 +700,112 @@ static int ensure_sampler(axbc_ctx *c, uint32_t nchecks)
     return AXBC_OK;
 }
 
+// One drawn round of one run: its pivots in passes of at most AXBC_W lanes;
+// the Bader replay of each pass sees the bc of the passes before it.
+static int sr_round_alone(axbc_ctx *c, SampledRun *r)
+{
+    const int nb = sr_nb(r);
+    for (int off = 0; off == 0 || off < nb; off += AXBC_W) {
+        const int cnt = std::min(nb - off, AXBC_W);
+        if (cnt > 0) {
+            TRY(sr_load(c, r, off, 0));
+            TRY(axbc_batch_traverse(c, cnt, r->prm.H));
+            r->batches++;
+            float *tg[AXBC_W];
+            for (int i = 0; i < AXBC_W; i++) tg[i] = r->bc;
+            TRY(axbc_batch_set_targets(c, tg));
+        }
+        TRY(sr_post(c, r, off, 0));
+        if (cnt > 0) {
+            float *dout[1] = {r->delta_last};
+            const int lo[1] = {0}, hi[1] = {AXBC_W};
+            TRY(axbc_batch_apply_lanes(c, dout, lo, hi, 1));
+        }
+        if (off + AXBC_W < nb) {
+            // a later pass runs only if Bader's test did not stop the round
+            CU(cudaMemcpyAsync(&r->ss_host->done, &r->ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               c->stream));
+            CU(cudaStreamSynchronize(c->stream));
+            if (r->ss_host->done) break;
+        }
+    }
+    return AXBC_OK;
+}
+
 extern "C" int axbc_run_sampled(axbc_ctx *c, const axbc_run_params *prm, axbc_run_result *res)
 {
     CHECK_ARG(c && prm && res, "axbc_run_sampled: null argument");
+    TRY(sr_check_params(c->g, prm, AXBC_MAX_WIDTH));
+    TRY(ensure_sampler(c, prm->nchecks));
+    // a view of the context's buffers
+    SampledRun r;
+    memset(&r, 0, sizeof(r));
+    r.prm = *prm;
+    r.ss = c->ss;
+    r.ss_host = c->ss_host;
+    r.bc = c->bc;
+    r.delta_last = c->delta_last;
+    r.used = c->used;
+    r.checks = c->checks;
+    r.checkval = c->checkval;
+    r.dyn_local = c->dyn_local;
+    r.dyn_csum = c->dyn_csum;
+    r.dyn_local2 = c->dyn_local2;
+    r.dyn_csum2 = c->dyn_csum2;
+    int st = sr_alloc_hist(&r, c->g->n);
+    if (st == AXBC_OK) st = sr_begin(c, &r);
+    while (st == AXBC_OK) {
+        if ((st = sr_draw(c, &r)) != AXBC_OK) break;
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            st = axbc_cuda_fail(cudaGetLastError(), "sampler", __FILE__, __LINE__);
+            break;
+        }
+        if (sr_finished(&r)) break;
+        st = sr_round_alone(c, &r);
+    }
+    if (st == AXBC_OK) st = sr_result(c, &r, res, &c->run_pivots, &c->run_probs, &c->run_checks);
+    sr_release(&r, false);
+    return st;
+}
+
+// ------------------------------------------------- single draws, stop test
+__global__ void k_sample_one(SamplerDists D, int z, uint64_t N, int first, double S_lcc,
+                             uint64_t *state, uint32_t *out_v, double *out_p)
+{
+    uint64_t x = state[0];
+    uint32_t mix = (uint32_t)state[1];
+    const uint64_t nbB = (N + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
+    double S_bc = 0, S_d = 0;
+    if (!first) {
+        if (D.bc_csum) S_bc = D.bc_csum[nbB - 1];
+        if (D.d_csum) S_d = D.d_csum[nbB - 1];
+    }
+    uint32_t v0 = 0;
+    double prob = 0;
+    d_draw_one(x, mix, z, N, D, first != 0, S_bc, S_d, S_lcc, v0, prob);
+    state[0] = x;
+    state[1] = mix;
+    *out_v = v0;
+    *out_p = prob;
+}
+
+extern "C" uint64_t axbc_srand48(int64_t seed)
+{
+    return (((uint64_t)seed & 0xffffffffULL) << 16) | 0x330EULL;
+}
+
+extern "C" int axbc_sample(axbc_ctx *c, int z, uint64_t *rng, uint32_t *mix, int first, uint32_t *v0,
+                           double *p)
+{
+    CHECK_ARG(c && rng && mix && v0 && p, "axbc_sample: null argument");
+    CHECK_ARG(z >= 0 && z <= 6, "axbc_sample: heuristic must be in [0,6]");
+    CHECK_ARG(z != 6 || *mix <= 4, "axbc_sample: mixture state must be in [0,4]");
+    TRY(ensure_sampler(c, 0));
     axbc_graph *g = c->g;
     const uint64_t n = g->n;
-    CHECK_ARG(prm->z >= 0 && prm->z <= 6, "axbc_run_sampled: heuristic must be in [0,6]");
-    CHECK_ARG(prm->H == 0 || prm->H == 1, "axbc_run_sampled: H must be 0 or 1");
-    CHECK_ARG(prm->batch_width >= 1 && prm->batch_width <= AXBC_MAX_WIDTH,
-              "axbc_run_sampled: batch_width must be in [1, 64]");
-    CHECK_ARG(prm->nchecks <= n, "axbc_run_sampled: more check vertices than vertices");
-    TRY(ensure_sampler(c, prm->nchecks));
     cudaStream_t s = c->stream;
-    const int z = prm->z;
     if (z == 1 || z == 6) TRY(axbc_build_deg_dist(g, s));
     if (z == 2 || z == 6) TRY(axbc_build_lcc(g, s));
-
-    const uint64_t nbfs = prm->nbfs < n ? prm->nbfs : n;
-    uint32_t *hist_v = nullptr;
-    double *hist_p = nullptr;
-    TRY(axbc_dalloc((void **)&hist_v, (nbfs + 1) * 4, nullptr));
-    TRY(axbc_dalloc((void **)&hist_p, (nbfs + 1) * 8, nullptr));
-
-    CU(cudaMemsetAsync(c->bc, 0, n * 4, s));
-    CU(cudaMemsetAsync(c->delta_last, 0, n * 4, s));
-    CU(cudaMemsetAsync(c->used, 0, n, s));
-    {
-        ProfScope ps(c, KP_SAMPLER, 0);
-        k_sampler_init<<<1, 1, 0, s>>>(c->ss, c->checks, prm->seed, z, prm->nbfs, n,
-                                       (uint32_t)prm->bader_c, prm->nchecks, prm->batch_width);
-    }
-    CU_LAUNCH("k_sampler_init");
-
     SamplerDists D;
     memset(&D, 0, sizeof(D));
     D.col = g->fwd.col;
@@ -500,93 +820,65 @@ extern "C" int axbc_run_sampled(axbc_ctx *c, const axbc_run_params *prm, axbc_ru
     D.lcc_csum = g->lcc_csum;
     D.bc = c->bc;
     D.delta_last = c->delta_last;
-    const bool dyn_bc = z == 3 || z == 5 || z == 6;
-    const bool dyn_d = z == 4 || z == 6;
-    if (dyn_bc) {
-        D.bc_local = c->dyn_local;
-        D.bc_csum = c->dyn_csum;
-    }
-    if (dyn_d) {
-        D.d_local = c->dyn_local2;
-        D.d_csum = c->dyn_csum2;
-    }
     const uint64_t nbB = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
     const unsigned hb = (unsigned)((nbB + 127) / 128);
-    int batches = 0;
-    for (;;) {
-        if (dyn_bc) {
-            ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
-            k_hprefix_local<<<hb, 128, 0, s>>>(c->bc, n, c->dyn_local, c->dyn_csum, z == 5 ? 1 : 0, c->ss);
-        }
-        if (dyn_bc) {
-            ProfScope ps(c, KP_SAMPLER, 0);
-            k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum, nbB, c->ss);
-        }
-        if (dyn_d) {
-            ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
-            k_hprefix_local<<<hb, 128, 0, s>>>(c->delta_last, n, c->dyn_local2, c->dyn_csum2, 0, c->ss);
-        }
-        if (dyn_d) {
-            ProfScope ps(c, KP_SAMPLER, 0);
-            k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum2, nbB, c->ss);
-        }
-        {
-            ProfScope ps(c, KP_SAMPLER, 0);
-            k_sampler<<<1, 1, 0, s>>>(c->ss, D, c->used, c->checks, g->S_lcc);
-        }
-        CU_LAUNCH("k_sampler");
-        CU(cudaMemcpyAsync(c->ss_host, c->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
-        CU(cudaStreamSynchronize(s));
-        const int nb = c->ss_host->nb;
-        if (c->ss_host->done && nb == 0 && c->ss_host->skipped_run == 0) break;
-        // the round's pivots in passes of at most AXBC_W lanes; the Bader
-        // replay of each pass sees the bc of the passes before it
-        for (int off = 0; off == 0 || off < nb; off += AXBC_W) {
-            const int cnt = std::min(nb - off, AXBC_W);
-            if (cnt > 0) {
-                k_load_pass<<<1, AXBC_W, 0, s>>>(c->ss, c->bi, off, 0);
-                CU_LAUNCH("k_load_pass");
-                TRY(axbc_batch_traverse(c, cnt, prm->H));
-                batches++;
-            }
-            {
-                ProfScope ps(c, KP_SAMPLER, 0);
-                k_sampler_post<<<1, 1, 0, s>>>(c->ss, c->bi, c->bc, c->mdelta, c->seen, g->reach,
-                                               c->checks, c->checkval, hist_v, hist_p, nbfs + 1, off, 0);
-            }
-            CU_LAUNCH("k_sampler_post");
-            if (cnt > 0) TRY(axbc_batch_apply(c));
-            if (off + AXBC_W < nb) {
-                // a later pass runs only if Bader's test did not stop the round
-                CU(cudaMemcpyAsync(&c->ss_host->done, &c->ss->done, sizeof(int32_t),
-                                   cudaMemcpyDeviceToHost, s));
-                CU(cudaStreamSynchronize(s));
-                if (c->ss_host->done) break;
-            }
-        }
+    if (!first && (z == 3 || z == 5 || z == 6)) {
+        D.bc_local = c->dyn_local;
+        D.bc_csum = c->dyn_csum;
+        k_hprefix_local<<<hb, 128, 0, s>>>(c->bc, n, c->dyn_local, c->dyn_csum, z == 5 ? 1 : 0, nullptr);
+        k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum, nbB, nullptr);
     }
-    CU(cudaMemcpyAsync(c->ss_host, c->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
-    CU(cudaStreamSynchronize(s));
-    const SamplerState &S = *c->ss_host;
-    res->nrounds = S.nrounds;
-    res->skipped = S.skipped;
-    res->dropped = S.dropped;
-    res->rounds = S.ui;
-    res->te = S.te;
-    res->stopped = S.stopped;
-    res->batches = batches;
-    const uint64_t k = std::min<uint64_t>(S.nrounds, nbfs + 1);
-    c->run_pivots.resize(k);
-    c->run_probs.resize(k);
-    c->run_checks.resize(prm->nchecks);
-    if (k) {
-        CU(cudaMemcpy(c->run_pivots.data(), hist_v, k * 4, cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(c->run_probs.data(), hist_p, k * 8, cudaMemcpyDeviceToHost));
+    if (!first && (z == 4 || z == 6)) {
+        D.d_local = c->dyn_local2;
+        D.d_csum = c->dyn_csum2;
+        k_hprefix_local<<<hb, 128, 0, s>>>(c->delta_last, n, c->dyn_local2, c->dyn_csum2, 0, nullptr);
+        k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum2, nbB, nullptr);
     }
-    if (prm->nchecks)
-        CU(cudaMemcpy(c->run_checks.data(), c->checks, prm->nchecks * 4, cudaMemcpyDeviceToHost));
-    axbc_dfree(hist_v);
-    axbc_dfree(hist_p);
+    // state, v0, p through the check-value scratch of the context
+    uint64_t *dstate = nullptr;
+    TRY(axbc_dalloc((void **)&dstate, 32, nullptr));
+    // the reference keeps dist_mix = z outside the -z 6 mixture
+    uint64_t h[4] = {*rng, z == 6 ? *mix : (uint32_t)z, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(dstate, h, 16, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        k_sample_one<<<1, 1, 0, s>>>(D, z, n, first, g->S_lcc, dstate, (uint32_t *)(dstate + 2),
+                                     (double *)(dstate + 3));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, dstate, 32, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    axbc_dfree(dstate);
+    if (e != cudaSuccess) return axbc_cuda_fail(e, "axbc_sample", __FILE__, __LINE__);
+    *rng = h[0];
+    if (z == 6) *mix = (uint32_t)h[1];
+    *v0 = (uint32_t)h[2];
+    memcpy(p, &h[3], 8);
+    return AXBC_OK;
+}
+
+__global__ void k_bader_check(const float *bc, const uint32_t *checks, uint32_t x, uint64_t N, uint32_t c,
+                              int *out)
+{
+    *out = d_bader(bc, checks, x, N, c) ? 1 : 0;
+}
+
+extern "C" int axbc_bader_check(axbc_ctx *c, const uint32_t *checks, uint32_t x, uint32_t bader_c,
+                                int *satisfied)
+{
+    CHECK_ARG(c && satisfied && (checks || x == 0), "axbc_bader_check: null argument");
+    TRY(ensure_sampler(c, x));
+    cudaStream_t s = c->stream;
+    if (x) CU(cudaMemcpyAsync(c->checks, checks, x * 4, cudaMemcpyHostToDevice, s));
+    int *d = nullptr;
+    TRY(axbc_dalloc((void **)&d, 4, nullptr));
+    k_bader_check<<<1, 1, 0, s>>>(c->bc, c->checks, x, c->g->n, bader_c, d);
+    int h = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    axbc_dfree(d);
+    if (e != cudaSuccess) return axbc_cuda_fail(e, "axbc_bader_check", __FILE__, __LINE__);
+    *satisfied = h;
     return AXBC_OK;
 }
 

@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no e2e pass")
     ap.add_argument("--skip-plain", action="store_true", help="profiling runs: no plain pass")
+    ap.add_argument("--workload", default="headline", choices=["headline", "serving"],
+                    help="serving: the request server on resident graphs (p50/p99 latency)")
+    ap.add_argument("--requests", type=int, default=48, help="serving: requests submitted")
+    ap.add_argument("--rate", type=float, default=2.0, help="serving: mean arrivals per second")
     ap.add_argument("--push-factor", type=float, default=None,
                     help="fixed batched push/pull factor instead of autotuning (profiling runs)")
     return ap.parse_args()
@@ -162,8 +166,82 @@ def oracle_sample(g_csc, pivots, probs, seconds, threads):
     return te / dt, k, dt
 
 
+def serve_bench(args):
+    """The request server under Poisson arrivals (seed 11) over resident graphs:
+    Kronecker scales 16, 18, 20, 22 (edgefactor 16) and a 1024x1024 grid.  Each
+    request picks a graph and a heuristic -z 0..5 uniformly, width 8, and either
+    a budget of -N pivots log-uniform in [64, 2048] or Bader's adaptive stop
+    (-c 1, -x uniform in 4..16, at most 2048 pivots).  Latency = finish - submit
+    on the server's steady clock; throughput = traversed edges of all requests
+    over the span from the first submit to the last finish."""
+    import numpy as np
+    import torch
+    import axbc_gb300 as ax
+    torch.cuda.init()
+    graphs = [("kronecker-s16", ax.Graph.rmat(16, 16, seed=16)),
+              ("kronecker-s18", ax.Graph.rmat(18, 16, seed=18)),
+              ("kronecker-s20", ax.Graph.rmat(20, 16, seed=20)),
+              ("kronecker-s22", ax.Graph.rmat(22, 16, seed=22)),
+              ("grid-1024", ax.Graph.grid(1024, 0.02, 1e-4, seed=7))]
+    srv = ax.Server()
+    gids = [srv.add_graph(G, H=0) for _, G in graphs]
+    rng = np.random.default_rng(11)
+    jobs = []
+    t = 0.0
+    for i in range(args.requests):
+        t += rng.exponential(1.0 / args.rate)
+        gi = int(rng.integers(len(graphs)))
+        z = int(rng.integers(0, 6))
+        if rng.random() < 0.5:
+            nbfs = int(round(np.exp(rng.uniform(np.log(64), np.log(2048)))))
+            c, x = 0, 1
+        else:
+            nbfs, c, x = 2048, 1, int(rng.integers(4, 17))
+        jobs.append((t, gi, z, nbfs, c, x, 1000 + i))
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    ids = []
+    for (ta, gi, z, nbfs, c, x, seed) in jobs:
+        d = ta - (time.perf_counter() - t0)
+        if d > 0:
+            time.sleep(d)
+        ids.append(srv.submit(gids[gi], z=z, nbfs=nbfs, bader_c=c, nchecks=x, H=0, seed=seed, W=8))
+    infos = [srv.wait(r) for r in ids]
+    clk = clocks.stop()
+    st = srv.stats()
+    failed = [i["error"] for i in infos if i["state"] != "done"]
+    lat = np.array([(i["finish_ns"] - i["submit_ns"]) / 1e9 for i in infos])
+    wait = np.array([(i["start_ns"] - i["submit_ns"]) / 1e9 for i in infos])
+    span = (max(i["finish_ns"] for i in infos) - min(i["submit_ns"] for i in infos)) / 1e9
+    te = sum(i["te"] for i in infos)
+    per_graph = {}
+    for (ta, gi, *_), i, l in zip(jobs, infos, lat):
+        per_graph.setdefault(graphs[gi][0], []).append(float(l))
+    out = {"metric": "serving p99 request latency", "value": float(np.percentile(lat, 99)),
+           "unit": "s", "n_gpus": 1, "higher_is_better": False, "impl": "gb300",
+           "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+           "mean_queue_wait_s": float(wait.mean()), "requests": len(infos),
+           "failed": len(failed), "throughput_te_per_s": te / span, "requests_per_s": len(infos) / span,
+           "span_s": span, "passes": st["passes"], "lanes_per_pass": st["lanes"] / max(1, st["passes"]),
+           "p50_by_graph_s": {k: float(np.median(v)) for k, v in per_graph.items()},
+           "dtype": "u32 path counts, f32 dependencies", "data": "synthetic (device R-MAT, grid)",
+           "config": {"workload": "serving: resident kronecker s16/s18/s20/s22 ef16 + grid 1024^2; "
+                                  "Poisson arrivals (seed 11); -z 0..5; width 8; -N log-uniform "
+                                  "64-2048 or -c 1 -x 4..16",
+                      "rate_per_s": args.rate, "requests": args.requests,
+                      "hbm_budget_bytes": st["budget"]},
+           "clocks": clk}
+    if failed:
+        out["errors"] = failed[:3]
+    print(json.dumps(out), flush=True)
+    srv.close()
+
+
 def main():
     args = parse()
+    if args.workload == "serving":
+        return serve_bench(args)
     from axbc_gb300 import sharding
     rank, world, local = sharding.env()
     import numpy as np

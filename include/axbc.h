@@ -198,6 +198,77 @@ typedef struct {
 } axbc_run_result;
 
 int axbc_run_sampled(axbc_ctx *ctx, const axbc_run_params *prm, axbc_run_result *res);
+/* ---- the sampler and the stop test, one call each ----
+ * axbc_srand48: the drand48 state srand48(seed) sets (the reference seeds with
+ * 4343543, src/axbc2d.c:2736).  axbc_sample: one draw of heuristic z
+ * (src/axbc2d.c:2873-3051) from the context's current bc and last dependency
+ * vector; *rng (drand48 state) and *mix (-z 6 mixture state, 0..4, ignored
+ * for other z; the reference starts it at uniform_int(4, 0)) advance in place;
+ * first = 1 before
+ * any pivot is applied (the dynamic heuristics then draw uniformly).  Rejection
+ * of repeated pivots and degree-0 roots is the caller's, as in the reference's
+ * loop.  axbc_bader_check: *satisfied = 1 if every check vertex v has
+ * bc[v] / 2 >= c * n (src/axbc2d.c:2846-2870). */
+uint64_t axbc_srand48(int64_t seed);
+int axbc_sample(axbc_ctx *ctx, int z, uint64_t *rng, uint32_t *mix, int first, uint32_t *v0,
+                double *p);
+int axbc_bader_check(axbc_ctx *ctx, const uint32_t *checks, uint32_t x, uint32_t c,
+                     int *satisfied);
+
+/* ---- request server (many sampled runs over resident graphs) ----
+ * The reference serves one job per process.  The server keeps graphs resident
+ * and runs submitted sampled runs (the parameters of axbc_run_sampled, widths
+ * 1..AXBC_MAX_BATCH) on one worker thread, packing the drawn rounds of the
+ * requests of one graph into the lanes of a shared multi-source pass.  Each
+ * request's bc, pivots and counters are bit-identical to axbc_run_sampled with
+ * the same parameters.  Admission: a request's device state must fit in the
+ * budget's remaining bytes; otherwise it waits in arrival order. */
+typedef struct axbc_server axbc_server;
+
+enum {
+    AXBC_REQ_QUEUED = 0,   /* waiting for admission */
+    AXBC_REQ_RUNNING = 1,  /* admitted; device state allocated */
+    AXBC_REQ_DONE = 2,     /* result held on the host until released */
+    AXBC_REQ_FAILED = 3
+};
+
+typedef struct {
+    int32_t state;            /* AXBC_REQ_* */
+    int32_t status;           /* AXBC_OK or the error of a failed request */
+    axbc_run_result result;   /* valid once done */
+    uint64_t bytes;           /* device bytes the request holds while running */
+    uint64_t submit_ns, start_ns, finish_ns;  /* steady clock */
+    char error[256];
+} axbc_request_info;
+
+typedef struct {
+    uint64_t budget, in_use;  /* request-state device bytes */
+    uint64_t queued, admitted, completed;
+    uint64_t passes, lanes;   /* multi-source passes run, lanes filled */
+} axbc_server_stats_t;
+
+/* hbm_budget: device bytes for request state (0: 80% of free memory now). */
+int axbc_server_create(uint64_t hbm_budget, axbc_server **server);
+/* Make graph g (owned by the caller, alive until the server is destroyed)
+ * resident; H is the graph's one-degree reduction (requests must match).
+ * Graphs are added before the first request. */
+int axbc_server_add_graph(axbc_server *server, axbc_graph *g, int H, int *graph_id);
+/* Queue a sampled run; AXBC_ERR_BUSY if it can never fit in the budget. */
+int axbc_request_submit(axbc_server *server, int graph_id, const axbc_run_params *prm,
+                        uint64_t *request_id);
+int axbc_request_poll(axbc_server *server, uint64_t request_id, axbc_request_info *info);
+/* Block until done or failed (timeout_ms < 0: no limit; AXBC_ERR_TIMEOUT). */
+int axbc_request_wait(axbc_server *server, uint64_t request_id, int64_t timeout_ms,
+                      axbc_request_info *info);
+/* A done request's bc (n floats) and applied pivots (up to cap, *count = all). */
+int axbc_request_result(axbc_server *server, uint64_t request_id, float *bc_host,
+                        uint32_t *pivots, double *probs, uint64_t cap, uint64_t *count);
+/* Forget a done, failed or still queued request (a running one: AXBC_ERR_STATE). */
+int axbc_request_release(axbc_server *server, uint64_t request_id);
+int axbc_server_stats(axbc_server *server, axbc_server_stats_t *stats);
+/* Drops queued requests, finishes admitted ones, frees everything. */
+int axbc_server_destroy(axbc_server *server);
+
 /* The pivots applied by the last sampled run, in order, with their p. */
 int axbc_get_pivots(const axbc_ctx *ctx, uint32_t *v0, double *p, uint64_t cap,
                     uint64_t *count);

@@ -310,3 +310,52 @@ def test_division_fast_path_is_exact(axbc):
         bad, slow = axbc.selftest_division(1 << 25, seed)
         assert bad == 0
         assert slow < (1 << 25) // 4  # the exact divide is the exception
+
+
+def _lrand48(x):
+    x = (0x5DEECE66D * x + 0xB) & ((1 << 48) - 1)
+    return x, x >> 17
+
+
+@pytest.mark.parametrize("z", [0, 1, 2, 3, 5])
+def test_sample_and_stop_primitives_rebuild_the_run(axbc, orc, z):
+    """axbc_sample + axbc_run_pivot + axbc_bader_check, driven by the
+    reference's round loop (src/axbc2d.c:2729-3156) written out here, give the
+    sampled run's pivots, probabilities and bc."""
+    H = 1 if z in (1, 3) else 0
+    g, G = make(axbc, orc, golden_edges(), 1024, True, H)
+    n, nbfs, seed, nchecks = 1024, 40, 77, 3
+    ctx = axbc.Context(G)
+    x = axbc.srand48(seed)
+    checks = []
+    for _ in range(nchecks):  # uniform_int(N, 0): lrand48 % (N + 1)
+        x, r = _lrand48(x)
+        checks.append(r % (n + 1))
+    if z == 0:
+        x, _ = _lrand48(x)
+    used = np.zeros(n + 1, bool)
+    deg = g.deg
+    piv, probs = [], []
+    for ui in range(nbfs):
+        while True:
+            v, p, x, _ = ctx.sample(z, x, 0, first=not piv)
+            if not (v < n and used[v]):
+                break
+        if v >= n or deg[v] == 0:
+            if v < n:
+                used[v] = True
+            continue
+        used[v] = True
+        ctx.run_pivot(v, p, H)
+        piv.append(v)
+        probs.append(p)
+    want = orc.run(g, z=z, nbfs=nbfs, bader_c=0, nchecks=nchecks, H=H, seed=seed, W=1)
+    assert np.array_equal(np.array(checks, np.uint32), want["checks"])
+    assert np.array_equal(np.array(piv, np.uint32), want["pivots"])
+    assert np.array_equal(np.array(probs), want["probs"])
+    assert_float_exact(ctx.bc(), want["bc"], "bc from the primitives")
+    # the stop test on that bc, against the oracle's arithmetic
+    bc = want["bc"]
+    for c in (0, 1, 2):
+        sat = all(float(bc[v]) / 2.0 >= c * n if v < n else 0.0 >= c * n for v in checks)
+        assert ctx.bader_check(checks, c) == sat
