@@ -115,6 +115,7 @@ _SIGS = {
                                        C.c_double, C.c_int, _P, _P, C.POINTER(PivotStats)]),
     "axbc_selftest_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_uint64)]),
+    "axbc_ctx_level_stats": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_int, C.POINTER(C.c_int)]),
     "axbc_srand48": (C.c_uint64, [C.c_int64]),
     "axbc_sample": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int,
                               C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
@@ -368,6 +369,19 @@ class Context:
         return dict(push_factor_single=t.push_factor_single,
                     push_factor_batch=t.push_factor_batch, batch_width=t.batch_width,
                     batch_te_per_s=t.batch_te_per_s, plain_te_per_s=t.plain_te_per_s)
+
+    def level_stats(self, max_levels=1 << 16):
+        """Per forward level of the last batch: dict of arrays count, te, push,
+        list_count, list_cap (list_count > list_cap: the level was scanned)."""
+        lv = C.c_int()
+        _check(lib().axbc_ctx_level_stats(self._h, None, None, None, None, None, 0, C.byref(lv)))
+        L = min(lv.value, max_levels)
+        out = dict(count=np.zeros(L, np.uint64), te=np.zeros(L, np.uint64), push=np.zeros(L, np.int32),
+                   list_count=np.zeros(L, np.uint32), list_cap=np.zeros(L, np.uint32))
+        _check(lib().axbc_ctx_level_stats(self._h, _ptr(out["count"]), _ptr(out["te"]), _ptr(out["push"]),
+                                          _ptr(out["list_count"]), _ptr(out["list_cap"]), L,
+                                          C.byref(lv)))
+        return out
 
     def sample(self, z, rng, mix=0, first=False):
         """One draw of heuristic z from this context's bc / last delta:

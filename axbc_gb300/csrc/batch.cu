@@ -18,7 +18,7 @@ static __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * AXB
 
 // resident blocks per SM the pull kernel is compiled for (its register budget)
 #ifndef AXBC_PULL_MIN_BLOCKS
-#define AXBC_PULL_MIN_BLOCKS 8
+#define AXBC_PULL_MIN_BLOCKS 6
 #endif
 
 // Per-level vertex lists: the vertices whose level-L mask is nonzero, appended
@@ -135,6 +135,14 @@ __device__ __forceinline__ uint32_t grab_unit(uint32_t *ctr)
     uint32_t t = 0;
     if (lane_id() == 0) t = atomicAdd(ctr, 1u);
     return __shfl_sync(FULL_MASK, t, 0);
+}
+
+// A level with fewer work units than the grid has warps lets only as many
+// warps as units reach the counter: ~10^4 warps contending for one address
+// would cost tens of microseconds on a small level.
+__device__ __forceinline__ uint32_t warp_global()
+{
+    return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 }
 
 __host__ __device__ __forceinline__ uint64_t n_units(const Adj &a)
@@ -272,6 +280,7 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
     const uint32_t *lst = level_list(ll, L - 1, lcnt);  // the frontier, when stored
     const uint32_t ent = list_unit(lcnt);
     const uint64_t nu = lst ? nhi + (lcnt + ent - 1) / ent : n_units(a);
+    if (warp_global() >= nu) return;  // fewer units than warps: no contention
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -400,20 +409,45 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
         sg[lane] = fm;
         sk[lane] = k;
         __syncwarp();
+        const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
+        const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
 #pragma unroll 1
-        for (int g = 0; g < 8; g++) {
-            if (!((act >> (4 * g)) & 0xfu)) continue;
-            uint32_t x[4];
+        for (int g = 0; g < 4; g++) {
+            if (!((act >> (8 * g)) & 0xffu)) continue;
+            uint32_t x[8], mor = 0;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t m = sg[4 * g + q];
-                x[q] = ((m >> lane) & 1u) ? msigma[row_base(su[4 * g + q]) + lane] : 0u;
+            for (int h = 0; h < 2; h++) {
+                const uint4 uu = su4[2 * g + h], mm = sg4[2 * g + h];
+                const uint32_t u4[4] = {uu.x, uu.y, uu.z, uu.w};
+                const uint32_t m4[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    x[4 * h + q] = ((m4[q] >> lane) & 1u) ? msigma[row_base(u4[q]) + lane] : 0u;
+                    mor |= m4[q];
+                }
+            }
+            const int k0 = (int)sk[8 * g], k7 = (int)sk[8 * g + 7];
+            if (k0 == k7) {
+                // all eight positions belong to one vertex (k is nondecreasing)
+                if (k0 != cur) {
+                    if (cur >= 0) {
+                        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+                        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
+                        if ((int)lane == cur) mine = fo;
+                    }
+                    cur = k0;
+                    acc = 0;
+                    fo = 0;
+                }
+                acc += ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
+                fo |= mor;
+                continue;
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t m = sg[4 * g + q];
+            for (int q = 0; q < 8; q++) {
+                const uint32_t m = sg[8 * g + q];
                 if (!m) continue;
-                const int kq = (int)sk[4 * g + q];
+                const int kq = (int)sk[8 * g + q];
                 if (kq != cur) {
                     if (cur >= 0) {
                         const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
@@ -446,6 +480,7 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
 {
     const unsigned lane = lane_id();
     const uint64_t nhi = rv.n_heavy_items, nu = n_units(rv);
+    if (warp_global() >= nu) return;  // fewer units than warps: no contention
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -752,6 +787,7 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
     const uint64_t nhi = a.n_heavy_items;
     const uint32_t ent = list_unit(lcnt);
     const uint64_t nu = lst ? nhi + (lcnt + ent - 1) / ent : n_units(a);
+    if (warp_global() >= nu) return;  // fewer units than warps: no contention
     for (;;) {
         const uint32_t t = grab_unit(ctr);
         if (t >= nu) break;
@@ -887,7 +923,8 @@ __device__ __forceinline__ void stage_rows(float (*rows)[33], const float *__res
 __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ mdelta,
                                                       const uint32_t *__restrict__ seen,
                                                       const uint32_t *__restrict__ reach, uint64_t n,
-                                                      const BatchInfo *__restrict__ bi)
+                                                      const BatchInfo *__restrict__ bi,
+                                                      float *__restrict__ delta_out)
 {
     __shared__ uint32_t s_root[AXBC_W], s_reach[AXBC_W], s_skip0[AXBC_W];
     __shared__ double s_p[AXBC_W];
@@ -941,6 +978,10 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
     if (amask == 0) return;
     const bool single = s_single != 0;
     const int slast = 31 - __clz(amask);
+    // delta_out (when given): the last applied pivot's dependencies, taken
+    // from the staged rows (k_extract_delta's rule)
+    const uint32_t dl_root = bi->root[slast];
+    const bool dl_root_done = (bi->depth0mask >> slast) & 1u;
     const unsigned lane = lane_id();
     const unsigned wid = threadIdx.x >> 5;
     const uint64_t stride = (uint64_t)gridDim.x * (UPD_TPB / 32) * 32;
@@ -968,6 +1009,10 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         }
         __syncwarp();
         const uint64_t v = base + lane;
+        if (delta_out && v < n) {
+            const bool have = v == dl_root ? dl_root_done : ((sv >> slast) & 1u) != 0u;
+            delta_out[v] = have ? s_rows[wid][buf][lane][slast] : __uint2float_rn(rv);
+        }
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
         if ((sv != 0u || rv != 0u) && single) {
@@ -1073,9 +1118,10 @@ static int ensure_level_tables(axbc_ctx *c)
     TRY(axbc_dalloc((void **)&c->d_level_te, AXBC_MAX_LEVELS * 8, &c->bytes));
     TRY(axbc_dalloc((void **)&c->d_level_cnt, AXBC_MAX_LEVELS * 8, &c->bytes));
     TRY(axbc_dalloc((void **)&c->d_level_mode, AXBC_MAX_LEVELS * 4, &c->bytes));
-    // level lists: room for every vertex about twice over; a level may hold
-    // up to n/8 vertices before it falls back to the task scan
-    c->lpool_cap = (uint32_t)std::min<uint64_t>(2 * c->g->n + 64, 0xffffffffull);
+    // level lists: a vertex joins a level's list once per distinct depth at
+    // which the batch's pivots reach it, so 32 n entries never run out; a
+    // level may hold up to n/8 vertices before it falls back to the task scan
+    c->lpool_cap = (uint32_t)std::min<uint64_t>((uint64_t)AXBC_W * c->g->n + 64, 0xffffffffull);
     TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)c->lpool_cap * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->lstart, AXBC_MAX_LEVELS * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->lcount, AXBC_MAX_LEVELS * 4, &c->bytes));
@@ -1385,11 +1431,14 @@ int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane
         c->upd_blocks_per_sm = std::max(1, b);
     }
     const int grid = axbc_grid_for(c, UPD_TPB, c->upd_blocks_per_sm);
+    const bool one_seg = nseg == 1 && (!lane_lo || lane_lo[0] == 0) && (!lane_hi || lane_hi[0] >= AXBC_W);
     {
         ProfScope ps(c, KP_UPDATE, (double)g->n * c->last_batch_nsrc * 20.0);
-        k_update_m<<<grid, UPD_TPB, 0, s>>>(c->mdelta, c->seen, g->reach, g->n, c->bi);
+        // one segment over all lanes: the update writes the last delta itself
+        k_update_m<<<grid, UPD_TPB, 0, s>>>(c->mdelta, c->seen, g->reach, g->n, c->bi,
+                                            one_seg ? (delta_out ? delta_out[0] : c->delta_last) : nullptr);
     }
-    for (int i = 0; i < nseg; i++) {
+    for (int i = 0; i < nseg && !one_seg; i++) {
         ProfScope ps(c, KP_UPDATE, 0);
         k_extract_delta<<<grid, 256, 0, s>>>(delta_out ? delta_out[i] : c->delta_last, c->mdelta,
                                               c->seen, g->reach, g->n, c->bi,
@@ -1397,6 +1446,26 @@ int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane
     }
     CU_LAUNCH("update");
     c->delta_last_valid = true;
+    return AXBC_OK;
+}
+
+// Per forward level of the last batch: vertices newly reached (over all
+// pivots), their degree sum, the direction (1 push), and the level's vertex
+// list (entries counted, capacity; count > capacity: the level was scanned).
+extern "C" int axbc_ctx_level_stats(axbc_ctx *c, uint64_t *count, uint64_t *te, int32_t *push,
+                                    uint32_t *list_count, uint32_t *list_cap, int max_levels,
+                                    int *levels)
+{
+    CHECK_ARG(c && levels, "axbc_ctx_level_stats: null argument");
+    const int L = std::min(c->last_batch_levels + 1, max_levels);
+    *levels = c->last_batch_levels + 1;
+    if (!c->d_level_cnt || L <= 0) return AXBC_OK;
+    CU(cudaStreamSynchronize(c->stream));
+    if (count) CU(cudaMemcpy(count, c->d_level_cnt, L * 8, cudaMemcpyDeviceToHost));
+    if (te) CU(cudaMemcpy(te, c->d_level_te, L * 8, cudaMemcpyDeviceToHost));
+    if (push) CU(cudaMemcpy(push, c->d_level_mode, L * 4, cudaMemcpyDeviceToHost));
+    if (list_count) CU(cudaMemcpy(list_count, c->lcount, L * 4, cudaMemcpyDeviceToHost));
+    if (list_cap) CU(cudaMemcpy(list_cap, c->lcap, L * 4, cudaMemcpyDeviceToHost));
     return AXBC_OK;
 }
 

@@ -9,7 +9,9 @@
 //
 // Admission: a request's device bytes (sr_bytes) must fit in what the budget
 // has left; requests wait in arrival order, and a smaller later one may pass
-// a larger one that does not fit yet.
+// a larger one that does not fit yet.  Scheduling: the graphs with admitted
+// requests take turns; on a graph, the rounds that have waited longest go
+// first into the next pass.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -78,6 +80,7 @@ struct axbc_server {
     bool running = false;  // the worker has started
     uint64_t next_id = 1;
     uint64_t passes = 0, lanes = 0, admitted = 0, completed = 0;
+    int rr = -1;  // worker: the graph served last
 };
 
 static void req_fail(axbc_server *S, Request *r, int st)
@@ -237,8 +240,19 @@ static void serve_loop(axbc_server *S)
             S->active.push_back(r);
         }
         if (S->active.empty()) continue;
-        // the graph of the longest-waiting active request goes next
-        const int gi = S->active.front()->graph;
+        // graphs with admitted requests take turns, one pass each, so a long
+        // request on one graph does not hold back the requests on the others
+        int gi = -1;
+        const int ng = (int)S->graphs.size();
+        for (int k = 1; k <= ng && gi < 0; k++) {
+            const int cand = (S->rr + k) % ng;
+            for (Request *r : S->active)
+                if (r->graph == cand) {
+                    gi = cand;
+                    break;
+                }
+        }
+        S->rr = gi;
         std::vector<Request *> runs;
         for (Request *r : S->active)
             if (r->graph == gi) runs.push_back(r);

@@ -308,6 +308,12 @@ int axbc_ctx_profile_read(axbc_ctx *ctx, double *ms, uint64_t *count, double *by
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
 
+/* Per forward level of the last batch (up to max_levels; *levels = all):
+ * vertices newly reached over all pivots, their degree sum, direction (1:
+ * push), and the level's vertex list (count > cap: the level was scanned). */
+int axbc_ctx_level_stats(axbc_ctx *ctx, uint64_t *count, uint64_t *te, int32_t *push,
+                         uint32_t *list_count, uint32_t *list_cap, int max_levels, int *levels);
+
 /* ---- diagnostics ----
  * The bc update computes float(double(x) / p) with a float two-product path
  * and falls back to the double divide near float rounding midpoints; this
