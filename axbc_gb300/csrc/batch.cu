@@ -16,9 +16,13 @@
 
 static __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * AXBC_W; }
 
-// resident blocks per SM the pull kernel is compiled for (its register budget)
+// resident blocks per SM the pull and backward kernels are compiled for
+// (their register budgets)
 #ifndef AXBC_PULL_MIN_BLOCKS
 #define AXBC_PULL_MIN_BLOCKS 6
+#endif
+#ifndef AXBC_BWD_MIN_BLOCKS
+#define AXBC_BWD_MIN_BLOCKS 8
 #endif
 
 // Per-level vertex lists: the vertices whose level-L mask is nonzero, appended
@@ -828,7 +832,7 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
 }
 
 // One backward depth, device-driven: d = bi->bd (a no-op once below 0).
-__global__ void __launch_bounds__(BATCH_TPB, 8) k_bwd_step(Adj a, const BatchInfo *__restrict__ bi,
+__global__ void __launch_bounds__(BATCH_TPB, AXBC_BWD_MIN_BLOCKS) k_bwd_step(Adj a, const BatchInfo *__restrict__ bi,
                                                         uint32_t *const *__restrict__ tab,
                                                         const uint32_t *__restrict__ msigma,
                                                         float *mdelta, float *mq, float *mpartial,
@@ -1185,10 +1189,17 @@ static int dyn_grid(axbc_ctx *c)
         CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_step, BATCH_TPB, 0));
         CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step, BATCH_TPB, 0));
         CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_fwd_pull_step, BATCH_TPB, 0));
-        c->dyn_blocks_per_sm = std::max(1, std::min(a, b));
+        c->dyn_blocks_per_sm = std::max(1, a);
         c->pull_blocks_per_sm = std::max(1, d);
+        c->bwd_blocks_per_sm = std::max(1, b);
     }
     return axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm);
+}
+
+static int bwd_grid(axbc_ctx *c)
+{
+    dyn_grid(c);
+    return axbc_grid_for(c, BATCH_TPB, c->bwd_blocks_per_sm);
 }
 
 static int pull_grid(axbc_ctx *c)
@@ -1215,7 +1226,7 @@ static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
 static void bwd_step_kernels(axbc_ctx *c, int dgrid)
 {
     axbc_graph *g = c->g;
-    k_bwd_step<<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
+    k_bwd_step<<<bwd_grid(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
                                                    c->mq, c->mpartial, g->reach, c->ctrs,
                                                    lists_of(c));
     if (g->fwd.n_heavy)
@@ -1392,7 +1403,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
             const double bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
             {
                 ProfScope ps(c, KP_BWD, bytes);
-                k_bwd_step<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
+                k_bwd_step<<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
                                                        c->mq, c->mpartial, g->reach, c->ctrs, ll);
             }
             if (g->fwd.n_heavy) {

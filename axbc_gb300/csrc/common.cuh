@@ -256,6 +256,7 @@ struct axbc_ctx {
     int dyn_blocks_per_sm = 0;  // resident blocks of the dynamic kernels
     int upd_blocks_per_sm = 0;  // resident blocks of the batched bc update
     int pull_blocks_per_sm = 0; // resident blocks of the forward pull kernel
+    int bwd_blocks_per_sm = 0;  // resident blocks of the backward kernel
 };
 
 // allocation with byte accounting

@@ -88,13 +88,22 @@ __global__ void k_hprefix_local(const float *__restrict__ w, uint64_t n, double 
     }
 }
 
+// The running sum of the block totals, left to right (one warp: 32 totals
+// load per step, every lane adds them in order, lane k keeps the k-th sum).
 __global__ void k_hprefix_csum(double *csum, uint64_t nb, const SamplerState *ss)
 {
     if (ss && (ss->done || ss->nrounds_snap == 0)) return;
+    const unsigned lane = threadIdx.x;
     double c = 0.0;
-    for (uint64_t b = 0; b < nb; b++) {
-        c = __dadd_rn(c, csum[b]);
-        csum[b] = c;
+    for (uint64_t base = 0; base < nb; base += 32) {
+        const double x = base + lane < nb ? csum[base + lane] : 0.0;
+        double mine = 0.0;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            c = __dadd_rn(c, __shfl_sync(FULL_MASK, x, k));
+            if ((int)lane == k) mine = c;
+        }
+        if (base + lane < nb) csum[base + lane] = mine;
     }
 }
 
@@ -102,7 +111,7 @@ int axbc_hprefix_launch(const float *w, uint64_t n, double *local, double *csum,
 {
     const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
     k_hprefix_local<<<(unsigned)((nb + 127) / 128), 128, 0, s>>>(w, n, local, csum, 0, nullptr);
-    k_hprefix_csum<<<1, 1, 0, s>>>(csum, nb, nullptr);
+    k_hprefix_csum<<<1, 32, 0, s>>>(csum, nb, nullptr);
     CU_LAUNCH("hprefix");
     return AXBC_OK;
 }
@@ -595,7 +604,7 @@ int sr_draw(axbc_ctx *c, SampledRun *r)
         }
         {
             ProfScope ps(c, KP_SAMPLER, 0);
-            k_hprefix_csum<<<1, 1, 0, s>>>(r->dyn_csum, nbB, r->ss);
+            k_hprefix_csum<<<1, 32, 0, s>>>(r->dyn_csum, nbB, r->ss);
         }
     }
     if (dyn_d) {
@@ -607,7 +616,7 @@ int sr_draw(axbc_ctx *c, SampledRun *r)
         }
         {
             ProfScope ps(c, KP_SAMPLER, 0);
-            k_hprefix_csum<<<1, 1, 0, s>>>(r->dyn_csum2, nbB, r->ss);
+            k_hprefix_csum<<<1, 32, 0, s>>>(r->dyn_csum2, nbB, r->ss);
         }
     }
     {
@@ -826,13 +835,13 @@ extern "C" int axbc_sample(axbc_ctx *c, int z, uint64_t *rng, uint32_t *mix, int
         D.bc_local = c->dyn_local;
         D.bc_csum = c->dyn_csum;
         k_hprefix_local<<<hb, 128, 0, s>>>(c->bc, n, c->dyn_local, c->dyn_csum, z == 5 ? 1 : 0, nullptr);
-        k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum, nbB, nullptr);
+        k_hprefix_csum<<<1, 32, 0, s>>>(c->dyn_csum, nbB, nullptr);
     }
     if (!first && (z == 4 || z == 6)) {
         D.d_local = c->dyn_local2;
         D.d_csum = c->dyn_csum2;
         k_hprefix_local<<<hb, 128, 0, s>>>(c->delta_last, n, c->dyn_local2, c->dyn_csum2, 0, nullptr);
-        k_hprefix_csum<<<1, 1, 0, s>>>(c->dyn_csum2, nbB, nullptr);
+        k_hprefix_csum<<<1, 32, 0, s>>>(c->dyn_csum2, nbB, nullptr);
     }
     // state, v0, p through the check-value scratch of the context
     uint64_t *dstate = nullptr;
