@@ -130,6 +130,8 @@ _SIGS = {
     "axbc_request_release": (C.c_int, [_P, C.c_uint64]),
     "axbc_server_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "axbc_server_destroy": (C.c_int, [_P]),
+    "axbc_server_graph_stats": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                          C.POINTER(C.c_uint64)]),
 }
 
 PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bwd",
@@ -497,6 +499,11 @@ class Server:
         st = ServerStats()
         _check(lib().axbc_server_stats(self._h, C.byref(st)))
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def graph_stats(self, graph_id):
+        p, l, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().axbc_server_graph_stats(self._h, graph_id, C.byref(p), C.byref(l), C.byref(b)))
+        return dict(passes=p.value, lanes=l.value, busy_s=b.value / 1e9)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -40,6 +40,7 @@ struct ServeGraph {
     axbc_graph *g;
     int H;
     axbc_ctx *ctx;  // the shared multi-source buffers of this graph
+    uint64_t passes = 0, lanes = 0, busy_ns = 0;  // worker's account (read under the mutex)
 };
 
 struct Request {
@@ -217,7 +218,13 @@ static void serve_loop(axbc_server *S)
         }
         for (Request *r : admit) {
             axbc_ctx *c = S->graphs[r->graph].ctx;
-            int st = sr_alloc(S->graphs[r->graph].g, &r->prm, &r->run);
+            // static heuristics (-z 0..2) draw from distributions no pivot
+            // changes, so without Bader's stop (whose round counter depends on
+            // where a round ends) the width only sets how many pivots share a
+            // pass: run them 32 wide (same pivots, bits and counters)
+            axbc_run_params prm = r->prm;
+            if (prm.z <= 2 && prm.bader_c == 0) prm.batch_width = AXBC_W;
+            int st = sr_alloc(S->graphs[r->graph].g, &prm, &r->run);
             if (st == AXBC_OK) {
                 r->allocated = true;
                 st = sr_begin(c, &r->run);
@@ -256,7 +263,16 @@ static void serve_loop(axbc_server *S)
         std::vector<Request *> runs;
         for (Request *r : S->active)
             if (r->graph == gi) runs.push_back(r);
+        const uint64_t t0 = now_ns();
+        const uint64_t lanes0 = S->lanes;
         const int st = serve_pass(S, gi, runs);
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            ServeGraph &G = S->graphs[gi];
+            G.busy_ns += now_ns() - t0;
+            G.lanes += S->lanes - lanes0;
+            if (S->lanes != lanes0) G.passes++;
+        }
         if (st != AXBC_OK) {
             // a failed pass fails the requests that were in it
             for (Request *r : runs) {
@@ -448,6 +464,19 @@ extern "C" int axbc_server_stats(axbc_server *S, axbc_server_stats_t *st)
     st->completed = S->completed;
     st->passes = S->passes;
     st->lanes = S->lanes;
+    return AXBC_OK;
+}
+
+extern "C" int axbc_server_graph_stats(axbc_server *S, int graph_id, uint64_t *passes, uint64_t *lanes,
+                                       uint64_t *busy_ns)
+{
+    CHECK_ARG(S, "axbc_server_graph_stats: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    CHECK_ARG(graph_id >= 0 && graph_id < (int)S->graphs.size(), "axbc_server_graph_stats: no such graph");
+    const ServeGraph &G = S->graphs[graph_id];
+    if (passes) *passes = G.passes;
+    if (lanes) *lanes = G.lanes;
+    if (busy_ns) *busy_ns = G.busy_ns;
     return AXBC_OK;
 }
 

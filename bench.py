@@ -225,6 +225,7 @@ def serve_bench(args):
            "failed": len(failed), "throughput_te_per_s": te / span, "requests_per_s": len(infos) / span,
            "span_s": span, "passes": st["passes"], "lanes_per_pass": st["lanes"] / max(1, st["passes"]),
            "p50_by_graph_s": {k: float(np.median(v)) for k, v in per_graph.items()},
+           "worker_by_graph": {graphs[i][0]: srv.graph_stats(g) for i, g in enumerate(gids)},
            "dtype": "u32 path counts, f32 dependencies", "data": "synthetic (device R-MAT, grid)",
            "config": {"workload": "serving: resident kronecker s16/s18/s20/s22 ef16 + grid 1024^2; "
                                   "Poisson arrivals (seed 11); -z 0..5; width 8; -N log-uniform "
@@ -272,10 +273,10 @@ def main():
                                W=args.width)
 
     seed = sharding.rank_seed(4343543, rank)
-    # autotune the direction-switch factors on 32 trial pivots (set-up, untimed)
+    # autotune the direction-switch factors on 64 trial pivots (set-up, untimed)
     deg = G.deg()
     rng = np.random.default_rng(1234)
-    trial = rng.choice(np.flatnonzero(deg > 0), size=32, replace=False).astype(np.uint32)
+    trial = rng.choice(np.flatnonzero(deg > 0), size=64, replace=False).astype(np.uint32)
     tuning = None
     if args.impl == "gb300" and args.push_factor is not None:
         ctx.set_tuning(32.0, args.push_factor)

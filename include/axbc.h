@@ -266,6 +266,9 @@ int axbc_request_result(axbc_server *server, uint64_t request_id, float *bc_host
 /* Forget a done, failed or still queued request (a running one: AXBC_ERR_STATE). */
 int axbc_request_release(axbc_server *server, uint64_t request_id);
 int axbc_server_stats(axbc_server *server, axbc_server_stats_t *stats);
+/* Per resident graph: passes run, lanes filled, worker time spent on it (ns). */
+int axbc_server_graph_stats(axbc_server *server, int graph_id, uint64_t *passes, uint64_t *lanes,
+                            uint64_t *busy_ns);
 /* Drops queued requests, finishes admitted ones, frees everything. */
 int axbc_server_destroy(axbc_server *server);
 

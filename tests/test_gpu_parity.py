@@ -359,3 +359,29 @@ def test_sample_and_stop_primitives_rebuild_the_run(axbc, orc, z):
     for c in (0, 1, 2):
         sat = all(float(bc[v]) / 2.0 >= c * n if v < n else 0.0 >= c * n for v in checks)
         assert ctx.bader_check(checks, c) == sat
+
+
+@pytest.mark.parametrize("z", [0, 1, 2])
+def test_static_heuristics_do_not_depend_on_width(axbc, orc, z):
+    """With a distribution no pivot changes, the width only groups the same pivot
+    sequence into passes: bc bits, pivots and counters are the same at every width
+    (the request server relies on this to run static requests 32 wide).  With
+    Bader's stop the applied pivots and bc still agree; only the round counter
+    depends on where the stopping round ends."""
+    H = 1 if z == 1 else 0
+    g, G = make(axbc, orc, golden_edges(), 1024, True, H)
+    ctx = axbc.Context(G)
+    # round limits below the number of vertices the heuristic can draw: past
+    # that, every round runs the reference's full rejection loop (N*N draws)
+    for c, x, nbfs, seed in ((0, 1, 200, 99), (1, 8, 300, 11)):
+        runs = {}
+        for W in (1, 8, 32, 64):
+            r = ctx.run_sampled(z=z, nbfs=nbfs, bader_c=c, nchecks=x, H=H, seed=seed, W=W)
+            runs[W] = (r, ctx.bc())
+        r1, bc1 = runs[1]
+        for W, (r, bc) in runs.items():
+            assert np.array_equal(r["pivots"], r1["pivots"]) and np.array_equal(r["probs"], r1["probs"])
+            keys = ("nrounds", "skipped", "dropped", "te", "stopped") + (("ui_end",) if c == 0 else ())
+            for k in keys:
+                assert r[k] == r1[k], (c, W, k)
+            assert np.array_equal(bc.view(np.uint32), bc1.view(np.uint32)), (c, W)
