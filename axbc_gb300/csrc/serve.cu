@@ -1,17 +1,17 @@
 // Request server: many sampled runs over resident graphs, batched across
 // requests.  The reference runs one job per process (src/axbc2d.c:2729-3156);
 // here every admitted request keeps its own sampler, bc, last delta and check
-// vertices on the device, and one worker thread packs the drawn rounds of the
-// requests of one graph into the lanes of a shared multi-source pass
-// (continuous batching).  A request's lanes are contiguous and in its pivot
+// vertices on the device, and each resident graph has a worker thread and a
+// stream that pack the drawn rounds of the graph's requests into the lanes of
+// a shared multi-source pass (continuous batching); passes on different graphs
+// overlap on the device.  A request's lanes are contiguous and in its pivot
 // order, its update goes to its own bc vector, and its Bader replay reads only
 // its own lanes, so every request gets the bits it would get alone.
 //
 // Admission: a request's device bytes (sr_bytes) must fit in what the budget
 // has left; requests wait in arrival order, and a smaller later one may pass
-// a larger one that does not fit yet.  Scheduling: the graphs with admitted
-// requests take turns; on a graph, the rounds that have waited longest go
-// first into the next pass.
+// a larger one that does not fit yet.  On a graph, the rounds that have
+// waited longest go first into the next pass.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -36,16 +36,24 @@ uint64_t now_ns()
         .count();
 }
 
+
+
+struct Request;
+
 struct ServeGraph {
-    axbc_graph *g;
-    int H;
-    axbc_ctx *ctx;  // the shared multi-source buffers of this graph
+    axbc_graph *g = nullptr;
+    int H = 0;
+    axbc_ctx *ctx = nullptr;  // the shared multi-source buffers of this graph
+    cudaStream_t stream = nullptr;
+    std::thread worker;             // drives this graph's passes on its own stream
+    std::vector<Request *> active;  // admitted requests; touched by this worker only
     uint64_t passes = 0, lanes = 0, busy_ns = 0;  // worker's account (read under the mutex)
 };
 
 struct Request {
     uint64_t id = 0;
     int graph = 0;
+    ServeGraph *G = nullptr;  // the graph's entry (stable; graphs are never removed)
     axbc_run_params prm{};
     int state = AXBC_REQ_QUEUED;
     int status = AXBC_OK;
@@ -68,20 +76,15 @@ struct Request {
 
 struct axbc_server {
     int device = 0;
-    cudaStream_t stream = nullptr;
     uint64_t budget = 0, in_use = 0;
-    std::vector<ServeGraph> graphs;
+    std::vector<std::unique_ptr<ServeGraph>> graphs;  // stable addresses for the workers
     std::mutex mu;
     std::condition_variable work_cv, done_cv;
     std::deque<uint64_t> queue;  // submitted, not admitted, in arrival order
     std::map<uint64_t, std::unique_ptr<Request>> reqs;
-    std::vector<Request *> active;  // admitted; touched by the worker only
-    std::thread worker;
     bool stop = false;
-    bool running = false;  // the worker has started
     uint64_t next_id = 1;
     uint64_t passes = 0, lanes = 0, admitted = 0, completed = 0;
-    int rr = -1;  // worker: the graph served last
 };
 
 static void req_fail(axbc_server *S, Request *r, int st)
@@ -97,10 +100,10 @@ static void req_fail(axbc_server *S, Request *r, int st)
 // result to host memory, device state freed, budget returned
 static void req_finish(axbc_server *S, Request *r)
 {
-    axbc_ctx *c = S->graphs[r->graph].ctx;
+    axbc_ctx *c = r->G->ctx;
     int st = sr_result(c, &r->run, &r->res, &r->pivots, &r->probs, nullptr);
     if (st == AXBC_OK) {
-        r->bc.resize(S->graphs[r->graph].g->n);
+        r->bc.resize(r->G->g->n);
         if (cudaMemcpy(r->bc.data(), r->run.bc, r->bc.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = axbc_cuda_fail(cudaGetLastError(), "request result", __FILE__, __LINE__);
     }
@@ -122,9 +125,8 @@ static void req_finish(axbc_server *S, Request *r)
 
 // One pass over graph gi: draw the rounds of its requests that need one,
 // then pack drawn rounds into the lanes of one multi-source pass.
-static int serve_pass(axbc_server *S, int gi, std::vector<Request *> &runs)
+static int serve_pass(axbc_server *S, ServeGraph &G, std::vector<Request *> &runs)
 {
-    ServeGraph &G = S->graphs[gi];
     axbc_ctx *c = G.ctx;
     bool drew = false;
     for (Request *r : runs)
@@ -137,7 +139,7 @@ static int serve_pass(axbc_server *S, int gi, std::vector<Request *> &runs)
     for (Request *r : runs) {
         if (r->need_draw) {
             r->need_draw = false;
-            r->drawn_at = S->passes;
+            r->drawn_at = G.passes;
             if (sr_finished(&r->run)) {
                 req_finish(S, r);
                 continue;
@@ -186,12 +188,22 @@ static int serve_pass(axbc_server *S, int gi, std::vector<Request *> &runs)
     std::lock_guard<std::mutex> lk(S->mu);
     S->passes++;
     S->lanes += lane;
+    G.lanes += lane;
     return AXBC_OK;
 }
 
-static void serve_loop(axbc_server *S)
+// The worker of graph gi: admits queued requests for its graph while the
+// budget allows, then runs passes over them on the graph's own stream, so
+// passes on different graphs overlap on the device.
+static void serve_graph_loop(axbc_server *S, int gi)
 {
     cudaSetDevice(S->device);
+    ServeGraph *Gp;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        Gp = S->graphs[gi].get();
+    }
+    ServeGraph &G = *Gp;
     for (;;) {
         std::vector<Request *> admit;
         {
@@ -200,10 +212,11 @@ static void serve_loop(axbc_server *S)
                 // admission in arrival order while the budget allows
                 for (auto it = S->queue.begin(); it != S->queue.end();) {
                     Request *r = S->reqs[*it].get();
-                    if (S->in_use + r->bytes <= S->budget) {
+                    if (r->graph == gi && S->in_use + r->bytes <= S->budget) {
                         S->in_use += r->bytes;
                         r->state = AXBC_REQ_RUNNING;
                         r->t_start = now_ns();
+                        r->worker_ref = true;
                         S->admitted++;
                         admit.push_back(r);
                         it = S->queue.erase(it);
@@ -211,23 +224,22 @@ static void serve_loop(axbc_server *S)
                         ++it;
                     }
                 }
-                if (!admit.empty() || !S->active.empty()) break;
+                if (!admit.empty() || !G.active.empty()) break;
                 if (S->stop) return;
                 S->work_cv.wait(lk);
             }
         }
         for (Request *r : admit) {
-            axbc_ctx *c = S->graphs[r->graph].ctx;
             // static heuristics (-z 0..2) draw from distributions no pivot
             // changes, so without Bader's stop (whose round counter depends on
             // where a round ends) the width only sets how many pivots share a
             // pass: run them 32 wide (same pivots, bits and counters)
             axbc_run_params prm = r->prm;
             if (prm.z <= 2 && prm.bader_c == 0) prm.batch_width = AXBC_W;
-            int st = sr_alloc(S->graphs[r->graph].g, &prm, &r->run);
+            int st = sr_alloc(G.g, &prm, &r->run);
             if (st == AXBC_OK) {
                 r->allocated = true;
-                st = sr_begin(c, &r->run);
+                st = sr_begin(G.ctx, &r->run);
             }
             if (st != AXBC_OK) {
                 if (r->allocated) sr_free(&r->run);
@@ -237,41 +249,24 @@ static void serve_loop(axbc_server *S)
                     S->in_use -= r->bytes;
                 }
                 req_fail(S, r, st);
-                continue;
             }
             r->need_draw = true;
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                r->worker_ref = true;
-            }
-            S->active.push_back(r);
+            G.active.push_back(r);
         }
-        if (S->active.empty()) continue;
-        // graphs with admitted requests take turns, one pass each, so a long
-        // request on one graph does not hold back the requests on the others
-        int gi = -1;
-        const int ng = (int)S->graphs.size();
-        for (int k = 1; k <= ng && gi < 0; k++) {
-            const int cand = (S->rr + k) % ng;
-            for (Request *r : S->active)
-                if (r->graph == cand) {
-                    gi = cand;
-                    break;
-                }
-        }
-        S->rr = gi;
-        std::vector<Request *> runs;
-        for (Request *r : S->active)
-            if (r->graph == gi) runs.push_back(r);
         const uint64_t t0 = now_ns();
-        const uint64_t lanes0 = S->lanes;
-        const int st = serve_pass(S, gi, runs);
+        uint64_t lanes0;
         {
             std::lock_guard<std::mutex> lk(S->mu);
-            ServeGraph &G = S->graphs[gi];
+            lanes0 = G.lanes;
+        }
+        std::vector<Request *> runs;
+        for (Request *r : G.active)
+            if (r->state == AXBC_REQ_RUNNING) runs.push_back(r);
+        const int st = runs.empty() ? AXBC_OK : serve_pass(S, G, runs);
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
             G.busy_ns += now_ns() - t0;
-            G.lanes += S->lanes - lanes0;
-            if (S->lanes != lanes0) G.passes++;
+            if (G.lanes != lanes0) G.passes++;
         }
         if (st != AXBC_OK) {
             // a failed pass fails the requests that were in it
@@ -288,7 +283,7 @@ static void serve_loop(axbc_server *S)
         }
         std::lock_guard<std::mutex> lk(S->mu);
         std::vector<Request *> keep;
-        for (Request *r : S->active) {
+        for (Request *r : G.active) {
             if (r->state == AXBC_REQ_RUNNING) {
                 keep.push_back(r);
                 continue;
@@ -296,7 +291,9 @@ static void serve_loop(axbc_server *S)
             r->worker_ref = false;
             if (r->released) S->reqs.erase(r->id);
         }
-        S->active.swap(keep);
+        G.active.swap(keep);
+        // room freed: the other graphs' workers may admit now
+        S->work_cv.notify_all();
     }
 }
 
@@ -305,7 +302,6 @@ extern "C" int axbc_server_create(uint64_t hbm_budget, axbc_server **out)
     CHECK_ARG(out, "axbc_server_create: null argument");
     auto S = std::make_unique<axbc_server>();
     CU(cudaGetDevice(&S->device));
-    CU(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
     if (hbm_budget == 0) {
         size_t fr = 0, tot = 0;
         CU(cudaMemGetInfo(&fr, &tot));
@@ -320,19 +316,22 @@ extern "C" int axbc_server_add_graph(axbc_server *S, axbc_graph *g, int H, int *
 {
     CHECK_ARG(S && g && graph_id, "axbc_server_add_graph: null argument");
     CHECK_ARG(H == 0 || H == 1, "axbc_server_add_graph: H must be 0 or 1");
-    {
-        std::lock_guard<std::mutex> lk(S->mu);
-        CHECK_ARG(!S->running, "axbc_server_add_graph: graphs are added before the first request");
-    }
-    axbc_ctx *c = nullptr;
-    TRY(axbc_ctx_create(g, S->stream, &c));
-    int st = axbc_ensure_batch(c);
+    auto G = std::make_unique<ServeGraph>();
+    G->g = g;
+    G->H = H;
+    CU(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    int st = axbc_ctx_create(g, G->stream, &G->ctx);
+    if (st == AXBC_OK) st = axbc_ensure_batch(G->ctx);
     if (st != AXBC_OK) {
-        axbc_ctx_destroy(c);
+        if (G->ctx) axbc_ctx_destroy(G->ctx);
+        cudaStreamDestroy(G->stream);
         return st;
     }
-    S->graphs.push_back({g, H, c});
-    *graph_id = (int)S->graphs.size() - 1;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->graphs.push_back(std::move(G));
+    const int gi = (int)S->graphs.size() - 1;
+    S->graphs[gi]->worker = std::thread(serve_graph_loop, S, gi);
+    *graph_id = gi;
     return AXBC_OK;
 }
 
@@ -340,12 +339,18 @@ extern "C" int axbc_request_submit(axbc_server *S, int graph_id, const axbc_run_
                                    uint64_t *request_id)
 {
     CHECK_ARG(S && prm && request_id, "axbc_request_submit: null argument");
-    CHECK_ARG(graph_id >= 0 && graph_id < (int)S->graphs.size(), "axbc_request_submit: no such graph");
-    const ServeGraph &G = S->graphs[graph_id];
+    ServeGraph *Gp = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        CHECK_ARG(graph_id >= 0 && graph_id < (int)S->graphs.size(), "axbc_request_submit: no such graph");
+        Gp = S->graphs[graph_id].get();
+    }
+    const ServeGraph &G = *Gp;
     TRY(sr_check_params(G.g, prm, AXBC_W));
     CHECK_ARG(prm->H == G.H, "axbc_request_submit: H differs from the graph's");
     auto r = std::make_unique<Request>();
     r->graph = graph_id;
+    r->G = Gp;
     r->prm = *prm;
     r->bytes = sr_bytes(G.g->n, prm);
     r->t_submit = now_ns();
@@ -359,10 +364,6 @@ extern "C" int axbc_request_submit(axbc_server *S, int graph_id, const axbc_run_
     *request_id = r->id;
     S->queue.push_back(r->id);
     S->reqs[r->id] = std::move(r);
-    if (!S->running) {
-        S->running = true;
-        S->worker = std::thread(serve_loop, S);
-    }
     S->work_cv.notify_all();
     return AXBC_OK;
 }
@@ -473,7 +474,7 @@ extern "C" int axbc_server_graph_stats(axbc_server *S, int graph_id, uint64_t *p
     CHECK_ARG(S, "axbc_server_graph_stats: null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     CHECK_ARG(graph_id >= 0 && graph_id < (int)S->graphs.size(), "axbc_server_graph_stats: no such graph");
-    const ServeGraph &G = S->graphs[graph_id];
+    const ServeGraph &G = *S->graphs[graph_id];  // under the mutex
     if (passes) *passes = G.passes;
     if (lanes) *lanes = G.lanes;
     if (busy_ns) *busy_ns = G.busy_ns;
@@ -489,11 +490,14 @@ extern "C" int axbc_server_destroy(axbc_server *S)
         S->queue.clear();  // queued requests are dropped; admitted ones finish
         S->work_cv.notify_all();
     }
-    if (S->worker.joinable()) S->worker.join();
+    for (auto &G : S->graphs)
+        if (G->worker.joinable()) G->worker.join();
     for (auto &kv : S->reqs)
         if (kv.second->allocated) sr_free(&kv.second->run);
-    for (auto &G : S->graphs) axbc_ctx_destroy(G.ctx);
-    if (S->stream) cudaStreamDestroy(S->stream);
+    for (auto &G : S->graphs) {
+        axbc_ctx_destroy(G->ctx);
+        cudaStreamDestroy(G->stream);
+    }
     delete S;
     return AXBC_OK;
 }

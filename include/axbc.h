@@ -218,8 +218,9 @@ int axbc_bader_check(axbc_ctx *ctx, const uint32_t *checks, uint32_t x, uint32_t
 /* ---- request server (many sampled runs over resident graphs) ----
  * The reference serves one job per process.  The server keeps graphs resident
  * and runs submitted sampled runs (the parameters of axbc_run_sampled, widths
- * 1..AXBC_MAX_BATCH) on one worker thread, packing the drawn rounds of the
- * requests of one graph into the lanes of a shared multi-source pass.  Each
+ * 1..AXBC_MAX_BATCH) with one worker thread and stream per graph, packing the
+ * drawn rounds of the requests of one graph into the lanes of a shared
+ * multi-source pass; passes on different graphs overlap on the device.  Each
  * request's bc, pivots and counters are bit-identical to axbc_run_sampled with
  * the same parameters.  Admission: a request's device state must fit in the
  * budget's remaining bytes; otherwise it waits in arrival order. */
@@ -250,8 +251,8 @@ typedef struct {
 /* hbm_budget: device bytes for request state (0: 80% of free memory now). */
 int axbc_server_create(uint64_t hbm_budget, axbc_server **server);
 /* Make graph g (owned by the caller, alive until the server is destroyed)
- * resident; H is the graph's one-degree reduction (requests must match).
- * Graphs are added before the first request. */
+ * resident, with its own stream and worker thread; H is the graph's one-degree
+ * reduction (requests must match). */
 int axbc_server_add_graph(axbc_server *server, axbc_graph *g, int H, int *graph_id);
 /* Queue a sampled run; AXBC_ERR_BUSY if it can never fit in the budget. */
 int axbc_request_submit(axbc_server *server, int graph_id, const axbc_run_params *prm,
