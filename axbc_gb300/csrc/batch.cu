@@ -37,24 +37,26 @@ struct LevelLists {
 };
 
 
-// Clear the level masks 2..lend of the previous batch (levels 0 and 1 are
-// cleared with memsets): a level whose list was stored has nonzero entries
-// only at its listed vertices; an overflowed level is cleared whole.
+// Clear the level masks first..last of the previous batch (levels 0 and 1
+// are cleared with memsets): a level whose list was stored has nonzero
+// entries only at its listed vertices; an overflowed level is cleared whole.
+// The grid walks the levels in order, all blocks sharing each level.
 __global__ void k_clean_levels(uint32_t *const *__restrict__ tab, const uint32_t *__restrict__ pool,
                                const uint32_t *__restrict__ lstart,
                                const uint32_t *__restrict__ lcount,
-                               const uint32_t *__restrict__ lcap, uint64_t n, int first)
+                               const uint32_t *__restrict__ lcap, uint64_t n, int first, int last)
 {
-    const int L = first + blockIdx.y;
-    uint32_t *f = tab[L];
-    const uint32_t cnt = lcount[L];
     const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
-    if (cnt <= lcap[L]) {
-        const uint32_t *lst = pool + lstart[L];
-        for (uint64_t i = tid; i < cnt; i += nt) f[lst[i]] = 0;
-    } else {
-        for (uint64_t i = tid; i < n; i += nt) f[i] = 0;
+    for (int L = first; L <= last; L++) {
+        uint32_t *f = tab[L];
+        const uint32_t cnt = lcount[L];
+        if (cnt <= lcap[L]) {
+            const uint32_t *lst = pool + lstart[L];
+            for (uint64_t i = tid; i < cnt; i += nt) f[lst[i]] = 0;
+        } else {
+            for (uint64_t i = tid; i < n; i += nt) f[i] = 0;
+        }
     }
 }
 
@@ -939,6 +941,7 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
     // division applies (bit 0) and zero terms may be skipped (bit 1)
     __shared__ float4 s_k[AXBC_W];
     __shared__ int s_single;  // every applied lane updates the same vector
+    __shared__ int s_allpos;  // every applied lane has p > 0 (zero terms vanish)
     // per warp, two chunks: the dependency rows of 32 vertices, padded to 33
     // floats so that thread t reading row t, column s hits bank (t + s) mod 32
     __shared__ float s_rows[UPD_TPB / 32][2][32][33];
@@ -968,19 +971,24 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         s_k[s] = make_float4(__uint2float_rn(s_reach[s] + 1u), iv.hi, iv.lo,
                              __uint_as_float((iv.ok ? 1u : 0u) | (s_skip0[s] ? 2u : 0u)));
         if (s == 0) {
-            int single = 1;
+            int single = 1, allpos = 1;
             float *t0 = nullptr;
             for (int l = 0; l < AXBC_W; l++)
                 if ((amask >> l) & 1u) {
                     if (!t0) t0 = bi->lane_bc[l];
                     else if (bi->lane_bc[l] != t0) single = 0;
+                    if (!(bi->p[l] > 0.0)) allpos = 0;
                 }
             s_single = single;
+            s_allpos = allpos;
         }
     }
     __syncthreads();
     if (amask == 0) return;
     const bool single = s_single != 0;
+    // a vertex no pivot reached, with reach 0, gets only zero terms: skipped
+    // when they vanish (p > 0; 0/0 is NaN, as in the reference)
+    const bool skip_unreached = s_allpos != 0;
     const int slast = 31 - __clz(amask);
     // delta_out (when given): the last applied pivot's dependencies, taken
     // from the staged rows (k_extract_delta's rule)
@@ -1019,7 +1027,8 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         }
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
-        if ((sv != 0u || rv != 0u) && single) {
+        const bool work = v < n && (sv != 0u || rv != 0u || !skip_unreached);
+        if (work && single) {
             // one target vector: all 32 lanes unrolled, lane order kept
             const float(*rows)[33] = s_rows[wid][buf];
             const float rf = __uint2float_rn(rv);
@@ -1039,7 +1048,7 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
                 b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
             }
             tgt[v] = b;
-        } else if (sv != 0u || rv != 0u) {
+        } else if (work) {
             const float(*rows)[33] = s_rows[wid][buf];
             const float rf = __uint2float_rn(rv);
             // lanes in order; consecutive lanes of one run add into one
@@ -1272,8 +1281,8 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     // the previous batch's level masks back to zero, then a larger list pool
     // if that batch ran out of list space
     if (c->prev_lend >= 2) {
-        dim3 cg(axbc_grid_for(c, 256, 2), c->prev_lend - 1);
-        k_clean_levels<<<cg, 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount, c->lcap, n, 2);
+        k_clean_levels<<<axbc_grid_for(c, 256, 2), 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount,
+                                                              c->lcap, n, 2, c->prev_lend);
         CU_LAUNCH("k_clean_levels");
         c->launches++;
     }
