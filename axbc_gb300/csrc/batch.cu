@@ -109,7 +109,13 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
         fd += __shfl_xor_sync(FULL_MASK, fd, o);
         rd += __shfl_xor_sync(FULL_MASK, rd, o);
     }
-    if (s < nsrc) ll.pool[s] = bi->root[s];
+    // the level-0 list: each root once (lanes of different runs may share one)
+    const uint32_t rt = s < nsrc ? bi->root[s] : 0xffffffffu;
+    const uint32_t same = __match_any_sync(FULL_MASK, rt);
+    const bool first = s < nsrc && (__ffs(same) - 1) == s;
+    const uint32_t firsts = __ballot_sync(FULL_MASK, first);
+    if (first) ll.pool[__popc(firsts & ((1u << s) - 1u))] = rt;
+    const uint32_t nroots = __popc(firsts);
     if (s < AXBC_W) bi->lane_bc[s] = bc;
     if (s == 0) {
         // a vertex counts as unvisited until every pivot has seen it: with one
@@ -122,10 +128,10 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
         level_te[0] = fd;
         level_cnt[0] = nsrc;
         ll.start[0] = 0;
-        ll.count[0] = nsrc;
-        ll.cap[0] = nsrc;
-        ll.start[1] = nsrc;
-        ll.cap[1] = min(list_max, pool_cap - nsrc);
+        ll.count[0] = nroots;
+        ll.cap[0] = nroots;
+        ll.start[1] = nroots;
+        ll.cap[1] = min(list_max, pool_cap - nroots);
     }
 }
 
@@ -1511,10 +1517,7 @@ extern "C" int axbc_run_batch(axbc_ctx *c, const uint32_t *v0, const double *p, 
     CHECK_ARG(c && v0 && p, "axbc_run_batch: null argument");
     CHECK_ARG(k >= 1 && k <= AXBC_MAX_BATCH, "axbc_run_batch: k must be in [1, 32]");
     CHECK_ARG(H == 0 || H == 1, "axbc_run_batch: H must be 0 or 1");
-    for (int i = 0; i < k; i++) {
-        CHECK_ARG(v0[i] < c->g->n, "axbc_run_batch: pivot >= n");
-        for (int j = 0; j < i; j++) CHECK_ARG(v0[i] != v0[j], "axbc_run_batch: repeated pivot");
-    }
+    for (int i = 0; i < k; i++) CHECK_ARG(v0[i] < c->g->n, "axbc_run_batch: pivot >= n");
     TRY(axbc_ensure_batch(c));
     cudaStream_t s = c->stream;
     for (int i = 0; i < k; i++) {

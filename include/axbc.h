@@ -165,8 +165,9 @@ int axbc_bc_pivot_static(const uint32_t *col, const uint32_t *row, const uint32_
 
 /* ---- batched (multi-source) form ----
  * k <= AXBC_MAX_BATCH pivots in one multi-source pass (one bit per pivot in a
- * 32-bit mask per vertex).  bc receives the pivots' updates in list order,
- * bit-identical to k calls of axbc_run_pivot.  stats may be NULL. */
+ * 32-bit mask per vertex; a pivot may repeat).  bc receives the pivots'
+ * updates in list order, bit-identical to k calls of axbc_run_pivot.  stats
+ * may be NULL. */
 int axbc_run_batch(axbc_ctx *ctx, const uint32_t *v0, const double *p, int k, int H,
                    axbc_pivot_stats *stats);
 

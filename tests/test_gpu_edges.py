@@ -1,10 +1,14 @@
 """Edge cases through the CUDA path, against the oracle: graphs without edges,
-graphs smaller than a batch, degree-0 roots, stars folded by the one-degree
-reduction, and the level limit of the batched traversal."""
+graphs smaller than a batch, degree-0 roots, repeated roots in one pass, stars
+folded by the one-degree reduction, and the level limit of the batched
+traversal."""
+import os
+
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
 def same_bits(got, want, what):
@@ -98,3 +102,20 @@ def test_level_limit_is_an_error_and_the_context_recovers(axbc, orc):
     ctx.run_batch(mid, np.array([1.0 / n, 1.0 / n]))
     want2, _, _ = orc.bc_pivots(g, mid, np.array([1.0 / n, 1.0 / n]))
     same_bits(ctx.bc(), want2, "batched pass after the error")
+
+
+def test_repeated_pivots_in_one_batch(axbc, orc):
+    """Lanes of different server requests can share a root: the level-0 list
+    holds each root once, every lane still counts its own paths."""
+    e = np.load(os.path.join(GOLDEN, "kron_s10_ef16.npz"))["edges"]
+    g, G = make(axbc, orc, e, 1024)
+    deg = g.deg
+    hub = int(np.argmax(deg))
+    other = int(np.flatnonzero(deg > 0)[3])
+    piv = np.array([hub, other, hub, hub, other, 5], np.uint32)
+    p = np.array([0.5, 0.25, 0.125, 0.5, 0.75, 1.0])
+    ctx = axbc.Context(G)
+    ctx.run_batch(piv, p)
+    want, dl, _ = orc.bc_pivots(g, piv, p)
+    same_bits(ctx.bc(), want, "bc with repeated roots")
+    same_bits(ctx.delta(), dl, "last delta")

@@ -128,3 +128,43 @@ def test_submit_errors_and_release(axbc, golden_graphs):
     with pytest.raises(axbc.AxbcError):
         srv.poll(rid)
     srv.close()
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_request_mixes(axbc, orc, seed):
+    """Random requests over three random graphs, submitted at once: each result
+    equals the oracle's run with the same parameters."""
+    rng = np.random.default_rng(seed)
+    srv = axbc.Server()
+    graphs = []
+    for k in range(3):
+        n = int(rng.integers(50, 600))
+        e = rng.integers(0, n, size=(int(rng.integers(n, 6 * n)), 2)).astype(np.uint64)
+        H = int(rng.random() < 0.5)
+        g = orc.pipeline(e, n, True, H)
+        G = axbc.Graph.from_csc(g.col, g.row, g.reach)
+        graphs.append((g, G, H, srv.add_graph(G, H=H)))
+    jobs = []
+    for _ in range(12):
+        gi = int(rng.integers(3))
+        g, G, H, gid = graphs[gi]
+        z = int(rng.integers(0, 7))
+        W = int(rng.choice([1, 4, 8, 16, 32]))
+        nbfs = int(rng.integers(1, min(g.n, 150)))
+        c, x = (0, 1) if rng.random() < 0.6 else (1, int(rng.integers(1, 5)))
+        sd = int(rng.integers(1, 1 << 30))
+        jobs.append((gi, z, W, nbfs, c, x, sd, srv.submit(gid, z=z, nbfs=nbfs, bader_c=c, nchecks=x,
+                                                            H=H, seed=sd, W=W)))
+    for gi, z, W, nbfs, c, x, sd, rid in jobs:
+        g, G, H, gid = graphs[gi]
+        info = srv.wait(rid, timeout_ms=120000)
+        assert info["state"] == "done", info["error"]
+        bc, piv, pr = srv.result(rid, G.n)
+        want = orc.run(g, z=z, nbfs=nbfs, bader_c=c, nchecks=x, H=H, seed=sd, W=W)
+        what = f"graph {gi} z={z} W={W} N={nbfs} c={c} x={x}"
+        assert np.array_equal(piv, want["pivots"]), what
+        assert np.array_equal(pr, want["probs"], equal_nan=True), what
+        for k in ("nrounds", "skipped", "dropped", "ui_end", "te", "stopped"):
+            assert info[k] == want[k], (what, k)
+        same_bits(bc, want["bc"], what)
+    srv.close()
