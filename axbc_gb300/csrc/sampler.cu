@@ -53,19 +53,21 @@ __device__ __forceinline__ int64_t d_lrand48(uint64_t &x)
     x = (0x5DEECE66DULL * x + 0xBULL) & 0xFFFFFFFFFFFFULL;
     return (int64_t)(x >> 17);
 }
-// uniform_int(max, min) in uint32 arithmetic (src/axbc2d.c:2155-2164)
-__device__ __forceinline__ uint32_t d_uniform_int(uint64_t &x, uint32_t max, uint32_t min)
+// uniform_int(max, min) in uint32 arithmetic (src/axbc2d.c:2155-2164), of the
+// lrand48 value r
+__device__ __forceinline__ uint32_t d_int_of(int64_t r, uint32_t max, uint32_t min)
 {
     const uint32_t mod = max - min + 1u;
-    const int64_t r = d_lrand48(x);
     if (mod == 0) return (uint32_t)r + min;
     return (uint32_t)(r % (int64_t)mod) + min;
 }
-// uniform01 (src/axbc2d.c:2172-2176): lrand48() / RAND_MAX
-__device__ __forceinline__ double d_uniform01(uint64_t &x)
+__device__ __forceinline__ uint32_t d_uniform_int(uint64_t &x, uint32_t max, uint32_t min)
 {
-    return __ddiv_rn((double)d_lrand48(x), 2147483647.0);
+    return d_int_of(d_lrand48(x), max, min);
 }
+// uniform01 (src/axbc2d.c:2172-2176): lrand48() / RAND_MAX
+__device__ __forceinline__ double d_01_of(int64_t r) { return __ddiv_rn((double)r, 2147483647.0); }
+__device__ __forceinline__ double d_uniform01(uint64_t &x) { return d_01_of(d_lrand48(x)); }
 
 // ------------------------------------------------- hierarchical prefix
 __global__ void k_hprefix_local(const float *__restrict__ w, uint64_t n, double *__restrict__ local,
@@ -207,59 +209,66 @@ __global__ void k_sampler_init(SamplerState *ss, uint32_t *checks, int64_t seed,
     ss->skipped_run = 0;
 }
 
-// One draw of heuristic z (dist_mix: the -z 6 mixture state): v0 and its
-// probability, the reference's rules of src/axbc2d.c:2873-3051.  snap0: no
-// pivot applied yet (the dynamic heuristics then draw uniformly).
+// The draws that take one lrand48 value: the pivot and its probability from
+// the value r, for the effective heuristic k in {0, 2, 3, 4, 5}.
+__device__ void d_map_one(int64_t r, int k, uint64_t N, const SamplerDists &D, bool snap0,
+                          double S_bc, double S_d, double S_lcc, uint32_t &v0, double &prob)
+{
+    int found;
+    if (k == 0 || snap0 && (k == 3 || k == 4 || k == 5)) {
+        v0 = d_int_of(r, (uint32_t)N, 0);
+        prob = __ddiv_rn(1.0, (double)N);
+    } else if (k == 2) {
+        // LCC (src/axbc2d.c:2919-2937)
+        const double rr = __dmul_rn(d_01_of(r), S_lcc);
+        uint64_t h = d_hsearch(D.lcc_local, D.lcc_csum, N, rr, &found);
+        if (!found) h = N - 1;
+        v0 = (uint32_t)h;
+        prob = __ddiv_rn((double)D.lcc[v0], S_lcc);
+    } else if (k == 4) {
+        // delta of the last pivot (src/axbc2d.c:2970-2991)
+        const double rr = __dmul_rn(d_01_of(r), S_d);
+        uint64_t h = d_hsearch(D.d_local, D.d_csum, N, rr, &found);
+        if (!found) h = N - 1;
+        v0 = (uint32_t)h;
+        prob = __ddiv_rn((double)D.delta_last[v0], S_d);
+    } else {
+        // bc (src/axbc2d.c:2941-2969) or 1/(1+bc) (2995-3022)
+        const double rr = __dmul_rn(d_01_of(r), S_bc);
+        uint64_t h = d_hsearch(D.bc_local, D.bc_csum, N, rr, &found);
+        if (!found) h = N - 1;
+        v0 = (uint32_t)h;
+        if (k == 3) prob = __ddiv_rn((double)D.bc[v0], S_bc);
+        else prob = __ddiv_rn(__ddiv_rn(1.0, __dadd_rn((double)D.bc[v0], 1.0)), S_bc);
+    }
+}
+
+// One draw of heuristic z (dist_mix: the -z 6 mixture state, equal to z for
+// the others): v0 and its probability, the reference's rules of
+// src/axbc2d.c:2873-3051.  snap0: no pivot applied yet (the dynamic heuristics
+// then draw uniformly).
 __device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, const SamplerDists &D,
                            bool snap0, double S_bc, double S_d, double S_lcc, uint32_t &v0,
                            double &prob)
 {
-    int found;
+    const int k = z == 6 ? (int)dist_mix : z;  // the distribution this draw uses
     prob = 0;
-    if (dist_mix == 0 || z == 0) {
-        v0 = d_uniform_int(x, (uint32_t)N, 0);
-        prob = __ddiv_rn(1.0, (double)N);
-    } else if (dist_mix == 1 || z == 1) {
-        // high-degree neighbourhood (src/axbc2d.c:2890-2917)
+    if (k == 1) {
+        // high-degree neighbourhood (src/axbc2d.c:2890-2917): one or two values
+        int found;
         const uint32_t r = d_uniform_int(x, D.sum_deg, 0);
         uint64_t h = d_find_u32(D.deg2p, D.seg_end, D.n_seg, r, &found);
         if (!found) h = N - 1;
         const uint32_t dh = D.col[h + 1] - D.col[h];
         if (dh > 0) {
-            uint32_t k = 0;
-            if (dh != 1) k = d_uniform_int(x, dh - 1, 0);
-            h = D.row[D.col[h] + k];
+            uint32_t kk = 0;
+            if (dh != 1) kk = d_uniform_int(x, dh - 1, 0);
+            h = D.row[D.col[h] + kk];
         }
         v0 = (uint32_t)h;
         prob = __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg);
-    } else if (dist_mix == 2 || z == 2) {
-        // LCC (src/axbc2d.c:2919-2937)
-        const double r = __dmul_rn(d_uniform01(x), S_lcc);
-        uint64_t h = d_hsearch(D.lcc_local, D.lcc_csum, N, r, &found);
-        if (!found) h = N - 1;
-        v0 = (uint32_t)h;
-        prob = __ddiv_rn((double)D.lcc[v0], S_lcc);
-    } else if (dist_mix == 3 || z == 3 || dist_mix == 4 || z == 4 || dist_mix == 5 || z == 5) {
-        const int kind = (dist_mix == 3 || z == 3) ? 3 : (dist_mix == 4 || z == 4) ? 4 : 5;
-        if (snap0) {
-            v0 = d_uniform_int(x, (uint32_t)N, 0);
-            prob = __ddiv_rn(1.0, (double)N);
-        } else if (kind == 4) {
-            // delta of the last pivot (src/axbc2d.c:2970-2991)
-            const double r = __dmul_rn(d_uniform01(x), S_d);
-            uint64_t h = d_hsearch(D.d_local, D.d_csum, N, r, &found);
-            if (!found) h = N - 1;
-            v0 = (uint32_t)h;
-            prob = __ddiv_rn((double)D.delta_last[v0], S_d);
-        } else {
-            // bc (src/axbc2d.c:2941-2969) or 1/(1+bc) (2995-3022)
-            const double r = __dmul_rn(d_uniform01(x), S_bc);
-            uint64_t h = d_hsearch(D.bc_local, D.bc_csum, N, r, &found);
-            if (!found) h = N - 1;
-            v0 = (uint32_t)h;
-            if (kind == 3) prob = __ddiv_rn((double)D.bc[v0], S_bc);
-            else prob = __ddiv_rn(__ddiv_rn(1.0, __dadd_rn((double)D.bc[v0], 1.0)), S_bc);
-        }
+    } else {
+        d_map_one(d_lrand48(x), k, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
     }
     if (z == 6) {
         // mixture probability (src/axbc2d.c:3026-3051)
@@ -279,18 +288,38 @@ __device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, c
         dist_mix = d_uniform_int(x, 2, 0);
     }
 }
-// Draw the rounds of one batch: up to W accepted pivots.
-__global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const uint32_t *checks,
-                          double S_lcc)
+
+// Draw the rounds of one batch: up to W accepted pivots.  Every thread of the
+// block runs the same sequential loop on the same values (stores by thread 0);
+// for the heuristics that take one lrand48 value per draw, a streak of
+// rejected draws (pivot already used) is searched SAMPLER_TPB draws at a time:
+// thread t evaluates the draw t steps ahead (drand48 skip-ahead: x -> A_t x +
+// C_t mod 2^48) and the first acceptable one wins, with the state and the
+// rejection count advanced exactly as the sequential loop would.
+#define SAMPLER_TPB 256
+__global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used,
+                                                       const uint32_t *checks, double S_lcc)
 {
-    ss->nb = 0;
-    ss->napply = 0;
-    ss->skipped_run = 0;
-    if (ss->done) return;
+    __shared__ uint64_t s_A[SAMPLER_TPB + 1], s_C[SAMPLER_TPB + 1];
+    __shared__ int s_best;
+    __shared__ uint32_t s_v0;
+    __shared__ double s_prob;
+    const int t = threadIdx.x;
+    const bool lead = t == 0;
+    const bool done = ss->done != 0;
+    __syncthreads();
+    if (lead) {
+        ss->nb = 0;
+        ss->napply = 0;
+        ss->skipped_run = 0;
+    }
+    if (done) return;
     const uint64_t N = ss->N;
     if (ss->bader_c > 0 && d_bader(D.bc, checks, ss->nchecks, N, ss->bader_c)) {
-        ss->stopped = 1;
-        ss->done = 1;
+        if (lead) {
+            ss->stopped = 1;
+            ss->done = 1;
+        }
         return;
     }
     uint64_t x = ss->rng;
@@ -298,50 +327,106 @@ __global__ void k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used, const
     const int z = ss->z;
     const uint32_t LIM = ss->lim;
     const bool snap0 = ss->nrounds_snap == 0;
+    const int W = ss->W;
+    const uint64_t nbfs = ss->nbfs;
     const uint64_t nbB = (N + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
     double S_bc = 0, S_d = 0;
     if (!snap0) {
         if (D.bc_csum) S_bc = D.bc_csum[nbB - 1];
         if (D.d_csum) S_d = D.d_csum[nbB - 1];
     }
+    const bool one_value = z == 0 || z == 2 || z == 3 || z == 4 || z == 5;
+    if (one_value && lead) {
+        const uint64_t M = 0xFFFFFFFFFFFFULL;
+        uint64_t A = 1, C = 0;
+        s_A[0] = 1;
+        s_C[0] = 0;
+        for (int k = 1; k <= SAMPLER_TPB; k++) {
+            A = (A * 0x5DEECE66DULL) & M;
+            C = (C * 0x5DEECE66DULL + 0xBULL) & M;
+            s_A[k] = A;
+            s_C[k] = C;
+        }
+    }
+    __syncthreads();
     int nb = 0;
     uint64_t ui = ss->ui, skipped_run = 0, dropped = 0;
-    while (nb < ss->W && ui < ss->nbfs) {
+    while (nb < W && ui < nbfs) {
         uint32_t v0 = 0;
         double prob = 0;
         uint32_t BSM = 0;
         bool good = false;
         while (!good) {
             if (BSM > LIM) break;
+            if (one_value && BSM >= 4) {
+                // candidates allowed before the bad-sample limit
+                const uint64_t allow = min((uint64_t)SAMPLER_TPB, (uint64_t)LIM - BSM + 1);
+                uint32_t v = 0;
+                double pr = 0;
+                bool acc = false;
+                if ((uint64_t)t < allow) {
+                    const uint64_t xt = (s_A[t + 1] * x + s_C[t + 1]) & 0xFFFFFFFFFFFFULL;
+                    d_map_one((int64_t)(xt >> 17), z, N, D, snap0, S_bc, S_d, S_lcc, v, pr);
+                    acc = !(v < N && used[v]);
+                }
+                if (lead) s_best = SAMPLER_TPB;
+                __syncthreads();
+                if (acc) atomicMin(&s_best, t);
+                __syncthreads();
+                const int j = s_best;
+                if (j < SAMPLER_TPB) {
+                    if (t == j) {
+                        s_v0 = v;
+                        s_prob = pr;
+                    }
+                    __syncthreads();
+                    v0 = s_v0;
+                    prob = s_prob;
+                    x = (s_A[j + 1] * x + s_C[j + 1]) & 0xFFFFFFFFFFFFULL;
+                    BSM += (uint32_t)j;
+                    good = true;
+                } else {
+                    x = (s_A[allow] * x + s_C[allow]) & 0xFFFFFFFFFFFFULL;
+                    BSM += (uint32_t)allow;
+                }
+                __syncthreads();
+                continue;
+            }
             d_draw_one(x, dist_mix, z, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
             if (v0 < N && used[v0]) BSM++;
             else good = true;
         }
-        if (BSM > LIM) {  // round dropped (src/axbc2d.c:3072-3077)
+        if (!good) {  // round dropped (src/axbc2d.c:3072-3077)
             dropped++;
             ui++;
             continue;
         }
         if (v0 >= N || D.col[v0 + 1] == D.col[v0]) {  // degree-0 root (3095-3111)
             skipped_run++;
-            if (v0 < N) used[v0] = 1;
+            if (v0 < N && lead) used[v0] = 1;
+            __syncthreads();
             ui++;
             continue;
         }
-        used[v0] = 1;
-        ss->v0[nb] = v0;
-        ss->p[nb] = prob;
-        ss->skip_before[nb] = skipped_run;
+        if (lead) {
+            used[v0] = 1;
+            ss->v0[nb] = v0;
+            ss->p[nb] = prob;
+            ss->skip_before[nb] = skipped_run;
+        }
+        __syncthreads();
         skipped_run = 0;
         nb++;
         ui++;
     }
-    ss->rng = x;
-    ss->dist_mix = dist_mix;
-    ss->ui = ui;
-    ss->nb = nb;
-    ss->skipped_run = skipped_run;
-    ss->dropped += dropped;
+    if (lead) {
+        ss->rng = x;
+        ss->dist_mix = dist_mix;
+        ss->ui = ui;
+        ss->nb = nb;
+        ss->skipped_run = skipped_run;
+        ss->dropped += dropped;
+    }
 }
 
 // Pivots [off, off + count) of a drawn round become lanes lane0 + 0.. of one
@@ -621,7 +706,7 @@ int sr_draw(axbc_ctx *c, SampledRun *r)
     }
     {
         ProfScope ps(c, KP_SAMPLER, 0);
-        k_sampler<<<1, 1, 0, s>>>(r->ss, D, r->used, r->checks, g->S_lcc);
+        k_sampler<<<1, SAMPLER_TPB, 0, s>>>(r->ss, D, r->used, r->checks, g->S_lcc);
     }
     CU_LAUNCH("k_sampler");
     CU(cudaMemcpyAsync(r->ss_host, r->ss, sizeof(SamplerState), cudaMemcpyDeviceToHost, s));
