@@ -117,6 +117,7 @@ _SIGS = {
                                          C.POINTER(C.c_uint64)]),
     "axbc_ctx_level_stats": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_int, C.POINTER(C.c_int)]),
     "axbc_srand48": (C.c_uint64, [C.c_int64]),
+    "axbc_inject_alloc_failures": (None, [C.c_int]),
     "axbc_sample": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int,
                               C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "axbc_bader_check": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(C.c_int)]),

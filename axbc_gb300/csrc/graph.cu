@@ -5,16 +5,27 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <vector>
 
 #include "common.cuh"
 
+// failure injection for tests: the next n device allocations fail
+static std::atomic<int> g_fail_allocs{0};
+
+extern "C" void axbc_inject_alloc_failures(int n) { g_fail_allocs.store(n < 0 ? 0 : n); }
+
 int axbc_dalloc(void **p, size_t bytes, uint64_t *acct)
 {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
+    for (int k = g_fail_allocs.load(); k > 0; k = g_fail_allocs.load())
+        if (g_fail_allocs.compare_exchange_weak(k, k - 1)) {
+            axbc_set_error("device allocation of %zu bytes refused (injected failure)", bytes);
+            return AXBC_ERR_NOMEM;
+        }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();

@@ -313,6 +313,10 @@ int axbc_ctx_profile_read(axbc_ctx *ctx, double *ms, uint64_t *count, double *by
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
 
+/* Test hook: the next n device allocations made by the library fail with
+ * AXBC_ERR_NOMEM (host-side failure injection; 0 clears it). */
+void axbc_inject_alloc_failures(int n);
+
 /* Per forward level of the last batch (up to max_levels; *levels = all):
  * vertices newly reached over all pivots, their degree sum, direction (1:
  * push), and the level's vertex list (count > cap: the level was scanned). */

@@ -168,3 +168,31 @@ def test_random_request_mixes(axbc, orc, seed):
             assert info[k] == want[k], (what, k)
         same_bits(bc, want["bc"], what)
     srv.close()
+
+
+def test_failed_request_releases_its_budget(axbc, golden_graphs):
+    """A request whose device state cannot be allocated (failure injected on the
+    host) fails with its status; the server goes on serving and its budget
+    account returns to zero."""
+    g, G = golden_graphs[0]
+    srv = axbc.Server()
+    gid = srv.add_graph(G, H=0)
+    axbc.lib().axbc_inject_alloc_failures(1)
+    bad = srv.submit(gid, z=3, nbfs=20, nchecks=1, seed=1, W=4)
+    info = srv.wait(bad, timeout_ms=60000)
+    axbc.lib().axbc_inject_alloc_failures(0)
+    assert info["state"] == "failed" and info["status"] == 3, info
+    assert "injected" in info["error"]
+    good = srv.submit(gid, z=3, nbfs=20, nchecks=1, seed=1, W=4)
+    assert srv.wait(good, timeout_ms=60000)["state"] == "done"
+    st = srv.stats()
+    assert st["in_use"] == 0 and st["completed"] == 1
+    srv.close()
+    # a context whose buffers cannot be allocated reports it; the next one works
+    axbc.lib().axbc_inject_alloc_failures(1)
+    with pytest.raises(axbc.AxbcError) as e:
+        axbc.Context(G)
+    axbc.lib().axbc_inject_alloc_failures(0)
+    assert e.value.status == 3
+    ctx = axbc.Context(G)
+    ctx.run_batch(np.array([1, 2], np.uint32), np.array([0.5, 0.5]))
