@@ -116,6 +116,7 @@ _SIGS = {
     "axbc_selftest_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_uint64)]),
     "axbc_ctx_level_stats": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_int, C.POINTER(C.c_int)]),
+    "axbc_ctx_profile_records": (C.c_int, [_P, _P, _P, _P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "axbc_srand48": (C.c_uint64, [C.c_int64]),
     "axbc_inject_alloc_failures": (None, [C.c_int]),
     "axbc_sample": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int,
@@ -405,6 +406,20 @@ class Context:
     def profile(self, enable=True):
         """Record CUDA events around every kernel launch of this context."""
         _check(lib().axbc_ctx_profile(self._h, int(enable)))
+
+    def profile_records(self):
+        """The timed launches since profile() / the last profile_read(), in order:
+        list of (kind, forward level or -1, ms, model bytes)."""
+        cnt = C.c_uint64()
+        _check(lib().axbc_ctx_profile_records(self._h, None, None, None, None, 0, C.byref(cnt)))
+        k = cnt.value
+        kinds = np.zeros(k, np.int32)
+        tags = np.zeros(k, np.int32)
+        ms = np.zeros(k, np.float32)
+        by = np.zeros(k, np.float64)
+        _check(lib().axbc_ctx_profile_records(self._h, _ptr(kinds), _ptr(tags), _ptr(ms), _ptr(by), k,
+                                              C.byref(cnt)))
+        return [(PROF_KINDS[a], int(b), float(c), float(d)) for a, b, c, d in zip(kinds, tags, ms, by)]
 
     def profile_read(self):
         """{kind: (ms, launches, algorithmic bytes)} since profile() / the last read."""

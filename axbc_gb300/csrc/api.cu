@@ -120,6 +120,32 @@ extern "C" int axbc_ctx_profile_read(axbc_ctx *c, double *ms, uint64_t *count, d
     return AXBC_OK;
 }
 
+// Every timed launch since profiling was enabled (or the last read), in
+// launch order: kind, forward level (-1: none), milliseconds, model bytes.
+// Reads up to cap records into the arrays (NULL: skip); *count = all records;
+// the records are kept (axbc_ctx_profile_read clears them).
+extern "C" int axbc_ctx_profile_records(axbc_ctx *c, int32_t *kinds, int32_t *tags, float *ms,
+                                        double *bytes, uint64_t cap, uint64_t *count)
+{
+    CHECK_ARG(c && count, "axbc_ctx_profile_records: null argument");
+    CU(cudaStreamSynchronize(c->stream));
+    uint64_t i = 0;
+    for (const ProfRec &r : c->prof) {
+        if (!r.a || !r.b) continue;
+        if (i < cap) {
+            float t = 0;
+            CU(cudaEventElapsedTime(&t, r.a, r.b));
+            if (kinds) kinds[i] = r.kind;
+            if (tags) tags[i] = r.tag;
+            if (ms) ms[i] = t;
+            if (bytes) bytes[i] = r.bytes;
+        }
+        i++;
+    }
+    *count = i;
+    return AXBC_OK;
+}
+
 extern "C" int axbc_ctx_launches(const axbc_ctx *c, uint64_t *launches)
 {
     CHECK_ARG(c && launches, "axbc_ctx_launches: null argument");
@@ -182,6 +208,7 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     axbc_dfree(c->lstart);
     axbc_dfree(c->lcount);
     axbc_dfree(c->lcap);
+    axbc_dfree(c->lheavy);
     if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
     if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
     axbc_dfree(c->mpartial);

@@ -34,6 +34,7 @@ struct LevelLists {
     uint32_t *start;  // per level: offset into pool
     uint32_t *count;  // per level: vertices appended
     uint32_t *cap;    // per level: capacity
+    uint32_t *heavy;  // per level: listed vertices with more than AXBC_SPAN neighbours
 };
 
 
@@ -64,7 +65,8 @@ __global__ void k_clean_levels(uint32_t *const *__restrict__ tab, const uint32_t
 __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t *fmask0, uint32_t *seen,
                              uint32_t *msigma, const uint32_t *__restrict__ col,
                              const uint32_t *__restrict__ rcol, unsigned long long m,
-                             double push_factor, unsigned long long *level_te,
+                             double push_factor, unsigned long long push_min,
+                             unsigned long long *level_te,
                              unsigned long long *level_cnt, LevelLists ll, uint32_t pool_cap,
                              uint32_t list_max)
 {
@@ -116,6 +118,8 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
     const uint32_t firsts = __ballot_sync(FULL_MASK, first);
     if (first) ll.pool[__popc(firsts & ((1u << s) - 1u))] = rt;
     const uint32_t nroots = __popc(firsts);
+    const uint32_t heavy_roots = __popc(__ballot_sync(FULL_MASK, first && col[rt + 1] - col[rt] > AXBC_SPAN));
+    if (s == 0) ll.heavy[0] = heavy_roots;
     if (s < AXBC_W) bi->lane_bc[s] = bc;
     if (s == 0) {
         // a vertex counts as unvisited until every pivot has seen it: with one
@@ -124,7 +128,8 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
         bi->front_deg = 0;
         bi->unvis_deg = unvis;
         bi->unvis_dec = 0;
-        bi->push_next = (double)fd * push_factor < (double)unvis;
+        bi->push_min = push_min;
+        bi->push_next = (double)fd * push_factor < (double)unvis || fd < push_min;
         level_te[0] = fd;
         level_cnt[0] = nsrc;
         ll.start[0] = 0;
@@ -287,9 +292,10 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
                                               int L)
 {
     const unsigned lane = lane_id();
-    const uint64_t nhi = a.n_heavy_items;
     uint32_t lcnt = 0;
     const uint32_t *lst = level_list(ll, L - 1, lcnt);  // the frontier, when stored
+    // heavy span items only when a heavy vertex is in the frontier
+    const uint64_t nhi = lst && ll.heavy[L - 1] == 0 ? 0 : a.n_heavy_items;
     const uint32_t ent = list_unit(lcnt);
     const uint64_t nu = lst ? nhi + (lcnt + ent - 1) / ent : n_units(a);
     if (warp_global() >= nu) return;  // fewer units than warps: no contention
@@ -601,6 +607,7 @@ __global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo 
     const uint64_t nblk = (items + 31) / 32;
     const uint64_t nw = nthreads / 32;
     unsigned long long cnt = 0, te = 0, rs = 0, fdeg = 0, udec = 0;
+    uint32_t hv = 0;  // heavy vertices of the level (their span items are scanned)
     bool any = false;
     for (uint64_t t = tid / 32; t < nblk; t += nw) {
         const uint64_t i = t * 32 + lane;
@@ -608,6 +615,7 @@ __global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo 
         if (i < items) {
             const uint64_t u = lst ? lst[i] : i;
             stats_vertex(u, srcmask, fcur, seen, col, rcol, reach, nm, d, r, fdeg, udec, any);
+            if (nm && d > AXBC_SPAN) hv++;
         }
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
@@ -625,8 +633,13 @@ __global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo 
     }
     {
         unsigned long long tsum = te;
-        for (int o = 16; o; o >>= 1) tsum += __shfl_xor_sync(FULL_MASK, tsum, o);
+        uint32_t hsum = hv;
+        for (int o = 16; o; o >>= 1) {
+            tsum += __shfl_xor_sync(FULL_MASK, tsum, o);
+            hsum += __shfl_xor_sync(FULL_MASK, hsum, o);
+        }
         if (lane == 0 && tsum) atomicAdd(&bi->lvl_te, tsum);
+        if (lane == 0 && hsum) atomicAdd(&ll.heavy[L], hsum);
     }
     if (cnt) {
         atomicAdd(&bi->lvl_new[lane], cnt);
@@ -670,7 +683,10 @@ __global__ void k_level_advance(BatchInfo *bi, unsigned long long *level_te,
         level_mode[L] = bi->push_next;
         bi->unvis_deg -= bi->unvis_dec;
         bi->unvis_dec = 0;
-        const bool push = (double)bi->front_deg * bi->push_factor < (double)bi->unvis_deg;
+        // push from a frontier whose degree sum is small against the graph:
+        // a pull would scan every vertex some pivot has not seen
+        const bool push = (double)bi->front_deg * bi->push_factor < (double)bi->unvis_deg ||
+                          bi->front_deg < bi->push_min;
         // where level L+1's list goes and how long it may grow
         const uint32_t used = ll.start[L] + (ll.count[L] <= ll.cap[L] ? ll.count[L] : 0u);
         ll.start[L + 1] = used;
@@ -793,10 +809,11 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
                                          float *mq, float *mpartial,
                                          const uint32_t *__restrict__ reach, uint32_t *ctr,
                                          uint32_t *su, uint32_t *sg, const uint32_t *lst,
-                                         uint32_t lcnt)
+                                         uint32_t lcnt, uint32_t lheavy)
 {
     const unsigned lane = lane_id();
-    const uint64_t nhi = a.n_heavy_items;
+    // heavy span items only when a heavy vertex is at this depth
+    const uint64_t nhi = lst && lheavy == 0 ? 0 : a.n_heavy_items;
     const uint32_t ent = list_unit(lcnt);
     const uint64_t nu = lst ? nhi + (lcnt + ent - 1) / ent : n_units(a);
     if (warp_global() >= nu) return;  // fewer units than warps: no contention
@@ -857,7 +874,7 @@ __global__ void __launch_bounds__(BATCH_TPB, AXBC_BWD_MIN_BLOCKS) k_bwd_step(Adj
     uint32_t lcnt = 0;
     const uint32_t *lst = level_list(ll, d, lcnt);
     bwd_body(a, dmask, d == bi->dmax, tab[d], tab[d + 1], msigma, mdelta, mq, mpartial, reach,
-             ctrs + 2 * d + 1, su, sg, lst, lcnt);
+             ctrs + 2 * d + 1, su, sg, lst, lcnt, ll.heavy[d]);
 }
 
 __device__ __forceinline__ void combine_body(const Adj &a, uint32_t dmask,
@@ -1145,12 +1162,13 @@ static int ensure_level_tables(axbc_ctx *c)
     TRY(axbc_dalloc((void **)&c->lstart, AXBC_MAX_LEVELS * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->lcount, AXBC_MAX_LEVELS * 4, &c->bytes));
     TRY(axbc_dalloc((void **)&c->lcap, AXBC_MAX_LEVELS * 4, &c->bytes));
+    TRY(axbc_dalloc((void **)&c->lheavy, AXBC_MAX_LEVELS * 4, &c->bytes));
     return AXBC_OK;
 }
 
 static LevelLists lists_of(const axbc_ctx *c)
 {
-    return LevelLists{c->lpool, c->lstart, c->lcount, c->lcap};
+    return LevelLists{c->lpool, c->lstart, c->lcount, c->lcap, c->lheavy};
 }
 
 static uint32_t list_max_of(const axbc_ctx *c)
@@ -1312,12 +1330,16 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     CU(cudaMemsetAsync(c->msigma, 0, n * AXBC_W * 4, s));
     CU(cudaMemsetAsync(c->ctrs, 0, 2 * AXBC_MAX_LEVELS * 4, s));
     CU(cudaMemsetAsync(c->lcount, 0, AXBC_MAX_LEVELS * 4, s));
+    CU(cudaMemsetAsync(c->lheavy, 0, AXBC_MAX_LEVELS * 4, s));
     const LevelLists ll = lists_of(c);
     const uint32_t lmax = list_max_of(c);
     {
         ProfScope ps(c, KP_LEVEL_STATS, 0);
         k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
-                                      g->rev.col, g->m, c->push_factor_batch, c->d_level_te,
+                                      g->rev.col, g->m, c->push_factor_batch,
+                                      // a factor of 1e30 or more pulls every level
+                                      c->push_factor_batch >= 1e30 ? 0ull : (unsigned long long)(n / 4),
+                                      c->d_level_te,
                                       c->d_level_cnt, ll, c->lpool_cap, lmax);
     }
     CU_LAUNCH("k_batch_init");
@@ -1418,6 +1440,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
             const double bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
             {
                 ProfScope ps(c, KP_BWD, bytes);
+                if (prof) c->prof.back().tag = d;
                 k_bwd_step<<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
                                                        c->mq, c->mpartial, g->reach, c->ctrs, ll);
             }

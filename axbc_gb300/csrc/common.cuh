@@ -146,6 +146,7 @@ struct BatchInfo {  // device, one multi-source batch
     int32_t bd;         // next backward depth (counts down to -1)
     int32_t push_next;  // 1: the next forward level pushes from the frontier
     double push_factor;
+    unsigned long long push_min;  // frontier degree sums below this always push
     int32_t Ls[AXBC_W];  // per pivot: first level that discovered nothing
     int32_t pool_short;  // a level's list was capped by the pool's size
     int32_t pad_;
@@ -217,7 +218,7 @@ struct axbc_ctx {
     unsigned long long *d_level_cnt = nullptr;  // per level: new (vertex, pivot) pairs
     int32_t *d_level_mode = nullptr;            // per level: 1 push, 0 pull
     uint32_t *lpool = nullptr;                  // per-level vertex lists
-    uint32_t *lstart = nullptr, *lcount = nullptr, *lcap = nullptr;
+    uint32_t *lstart = nullptr, *lcount = nullptr, *lcap = nullptr, *lheavy = nullptr;
     uint32_t lpool_cap = 0;
     bool pool_short = false;  // the last batch ran out of list space
     int prev_lend = 0;        // levels of the last batch whose masks need clearing

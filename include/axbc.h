@@ -111,13 +111,15 @@ int axbc_ctx_bytes(const axbc_ctx *ctx, uint64_t *bytes);
 
 /* Tuning knobs (autotuner output).  push_factor: a forward level pushes from
  * the frontier when frontier_edges * push_factor < unvisited_edges, else it
- * pulls into unvisited vertices.  Defaults are built in. */
+ * pulls into unvisited vertices; a batched level also pushes when its
+ * frontier's degree sum is below n/4, unless push_factor_batch >= 1e30 (every
+ * level pulls).  Defaults are built in. */
 int axbc_ctx_set_tuning(axbc_ctx *ctx, double push_factor_single, double push_factor_batch);
 
-/* Autotuner: times trial passes from the given pivots (the first 32 batched,
- * the first 4 plain) over a grid of direction-switch factors and batch
- * widths, keeps the fastest setting in the context and returns it.  bc is
- * reset to zero afterwards. */
+/* Autotuner: times trial passes from the given pivots (up to 128 batched, in
+ * batches of the width; the first 4 plain) over a grid of direction-switch
+ * factors and batch widths, keeps the fastest setting in the context and
+ * returns it.  bc is reset to zero afterwards. */
 typedef struct {
     double push_factor_single;
     double push_factor_batch;
@@ -310,6 +312,11 @@ int axbc_ctx_sync(axbc_ctx *ctx);
 int axbc_ctx_profile(axbc_ctx *ctx, int enable);
 /* per kind: total milliseconds, launches, algorithmic bytes; clears the records */
 int axbc_ctx_profile_read(axbc_ctx *ctx, double *ms, uint64_t *count, double *bytes, int nkinds);
+/* The individual timed launches, in order: kind (AXBC_PROF_KINDS order),
+ * forward level (-1: none), ms and model bytes; up to cap records, *count =
+ * all; the records stay (axbc_ctx_profile_read clears them). */
+int axbc_ctx_profile_records(axbc_ctx *ctx, int32_t *kinds, int32_t *tags, float *ms, double *bytes,
+                             uint64_t cap, uint64_t *count);
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
 
