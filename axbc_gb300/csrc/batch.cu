@@ -901,10 +901,12 @@ __global__ void k_bwd_combine_step(Adj a, const BatchInfo *__restrict__ bi,
                                    uint32_t *const *__restrict__ tab,
                                    const uint32_t *__restrict__ msigma, float *mdelta, float *mq,
                                    const float *__restrict__ mpartial,
-                                   const uint32_t *__restrict__ reach)
+                                   const uint32_t *__restrict__ reach, LevelLists ll)
 {
     const int d = bi->bd;
     if (d < 0) return;
+    uint32_t lcnt;
+    if (level_list(ll, d, lcnt) && ll.heavy[d] == 0) return;  // no heavy vertex at this depth
     const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
     if (!dmask) return;
     combine_body(a, dmask, tab[d], msigma, mdelta, mq, mpartial, reach);
@@ -1051,7 +1053,27 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
         const bool work = v < n && (sv != 0u || rv != 0u || !skip_unreached);
-        if (work && single) {
+        if (work && single && rv == 0u && skip_unreached) {
+            // one target vector, reach 0, every p > 0: a pivot that did not
+            // reach v adds +0, so only the reached lanes are visited, in lane
+            // order (roots are reached by their own lane)
+            const float(*rows)[33] = s_rows[wid][buf];
+            float *tgt = s_bc[slast];
+            float b = tgt[v];
+            for (uint32_t bits = sv & amask; bits; bits &= bits - 1u) {
+                const int s = __ffs(bits) - 1;
+                if ((uint32_t)v == s_root[s]) {
+                    if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
+                    continue;
+                }
+                const float dv = rows[lane][s];
+                if (dv == 0.0f) continue;
+                const float4 k = s_k[s];
+                const uint32_t fl = __float_as_uint(k.w);
+                b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
+            }
+            tgt[v] = b;
+        } else if (work && single) {
             // one target vector: all 32 lanes unrolled, lane order kept
             const float(*rows)[33] = s_rows[wid][buf];
             const float rf = __uint2float_rn(rv);
@@ -1264,7 +1286,8 @@ static void bwd_step_kernels(axbc_ctx *c, int dgrid)
                                                    lists_of(c));
     if (g->fwd.n_heavy)
         k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, c->stream>>>(
-            g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach);
+            g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach,
+            lists_of(c));
     k_bwd_advance<<<1, 1, 0, c->stream>>>(c->bi);
 }
 
@@ -1447,7 +1470,8 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
             if (g->fwd.n_heavy) {
                 ProfScope ps(c, KP_BWD_COMBINE, 0);
                 k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, s>>>(
-                    g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach);
+                    g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach,
+            lists_of(c));
             }
             k_bwd_advance<<<1, 1, 0, s>>>(c->bi);
             c->launches++;
