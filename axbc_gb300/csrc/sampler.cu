@@ -297,6 +297,16 @@ __device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, c
 // C_t mod 2^48) and the first acceptable one wins, with the state and the
 // rejection count advanced exactly as the sequential loop would.
 #define SAMPLER_TPB 256
+// rejections in a row before the block searches draws in parallel
+#ifndef AXBC_SAMPLER_STREAK
+#define AXBC_SAMPLER_STREAK 4
+#endif
+
+// The used-pivot flags are set by thread 0 between two barriers: after every
+// thread has tested the round's draws against them, before any thread tests
+// the next round's.
+__device__ __forceinline__ bool is_used(const uint8_t *used, uint32_t v) { return used[v] != 0; }
+__device__ __forceinline__ void set_used(uint8_t *used, uint32_t v) { used[v] = 1; }
 __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, SamplerDists D, uint8_t *used,
                                                        const uint32_t *checks, double S_lcc)
 {
@@ -358,7 +368,7 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
         bool good = false;
         while (!good) {
             if (BSM > LIM) break;
-            if (one_value && BSM >= 4) {
+            if (one_value && BSM >= AXBC_SAMPLER_STREAK) {
                 // candidates allowed before the bad-sample limit
                 const uint64_t allow = min((uint64_t)SAMPLER_TPB, (uint64_t)LIM - BSM + 1);
                 uint32_t v = 0;
@@ -367,7 +377,7 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
                 if ((uint64_t)t < allow) {
                     const uint64_t xt = (s_A[t + 1] * x + s_C[t + 1]) & 0xFFFFFFFFFFFFULL;
                     d_map_one((int64_t)(xt >> 17), z, N, D, snap0, S_bc, S_d, S_lcc, v, pr);
-                    acc = !(v < N && used[v]);
+                    acc = !(v < N && is_used(used, v));
                 }
                 if (lead) s_best = SAMPLER_TPB;
                 __syncthreads();
@@ -393,7 +403,7 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
                 continue;
             }
             d_draw_one(x, dist_mix, z, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
-            if (v0 < N && used[v0]) BSM++;
+            if (v0 < N && is_used(used, v0)) BSM++;
             else good = true;
         }
         if (!good) {  // round dropped (src/axbc2d.c:3072-3077)
@@ -401,15 +411,18 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
             ui++;
             continue;
         }
+        // every thread has tested this round's draws against the flags
+        // before thread 0 sets the new one
+        __syncthreads();
         if (v0 >= N || D.col[v0 + 1] == D.col[v0]) {  // degree-0 root (3095-3111)
             skipped_run++;
-            if (v0 < N && lead) used[v0] = 1;
+            if (v0 < N && lead) set_used(used, v0);
             __syncthreads();
             ui++;
             continue;
         }
         if (lead) {
-            used[v0] = 1;
+            set_used(used, v0);
             ss->v0[nb] = v0;
             ss->p[nb] = prob;
             ss->skip_before[nb] = skipped_run;
