@@ -336,45 +336,18 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
 // Forward level L, pull into vertex u for the pivots `ns` that have not seen
 // it: sum sigma_s over every in-neighbour at depth L-1 from pivot s (u32 sums:
 // any order gives the same bits).  The positions of a 32-wide chunk are staged
-// in shared memory.  Gathers use a pivot-quad layout: lane l serves position
-// slot g = l / 8 of each 4-position step and pivots 4j..4j+3 (j = l mod 8) with
-// one 16-byte load of the parent's sigma row, so one load instruction covers
-// four positions; per-slot partial sums are added across slots when a vertex
-// is written.
-__device__ __forceinline__ void quad_add(uint4 &acc, const uint32_t *__restrict__ msigma, uint32_t u,
-                                         uint32_t m, unsigned j)
-{
-    const uint32_t nib = (m >> (4 * j)) & 0xFu;
-    if (nib) {
-        const uint4 x = reinterpret_cast<const uint4 *>(msigma)[(uint64_t)u * (AXBC_W / 4) + j];
-        if (nib & 1u) acc.x += x.x;
-        if (nib & 2u) acc.y += x.y;
-        if (nib & 4u) acc.z += x.z;
-        if (nib & 8u) acc.w += x.w;
-    }
-}
-
-// the four slots' partial sums added up (every lane ends with the total)
-__device__ __forceinline__ uint4 quad_total(uint4 a)
-{
-#pragma unroll
-    for (int o = 8; o < 32; o <<= 1) {
-        a.x += __shfl_xor_sync(FULL_MASK, a.x, o);
-        a.y += __shfl_xor_sync(FULL_MASK, a.y, o);
-        a.z += __shfl_xor_sync(FULL_MASK, a.z, o);
-        a.w += __shfl_xor_sync(FULL_MASK, a.w, o);
-    }
-    return a;
-}
-
+// in shared memory; each 8-position group with a hit issues its eight gathers
+// before any is consumed.
 __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32_t b0, uint32_t b1,
                                               const uint32_t *__restrict__ fprev,
                                               const uint32_t *__restrict__ msigma, uint32_t *su,
-                                              uint32_t *sg, uint4 &acc)
+                                              uint32_t *sg, uint32_t &acc)
 {
-    const unsigned lane = lane_id(), g = lane >> 3, j = lane & 7u;
+    const unsigned lane = lane_id();
+    const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
+    const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
     uint32_t found = 0;
-    acc = make_uint4(0, 0, 0, 0);
+    acc = 0;
     // the next chunk's adjacency entries load while this chunk is consumed
     uint32_t vn = b0 + lane < b1 ? rv.row[b0 + lane] : 0u;
     for (uint32_t base = b0; base < b1; base += 32) {
@@ -389,10 +362,20 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
         sg[lane] = fm;
         __syncwarp();
 #pragma unroll 1
-        for (int g8 = 0; g8 < 4; g8++) {
-            if (!((act >> (8 * g8)) & 0xffu)) continue;
-            quad_add(acc, msigma, su[8 * g8 + g], sg[8 * g8 + g], j);
-            quad_add(acc, msigma, su[8 * g8 + g + 4], sg[8 * g8 + g + 4], j);
+        for (int g = 0; g < 4; g++) {
+            if (!((act >> (8 * g)) & 0xffu)) continue;
+            uint32_t x[8];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint4 ua = su4[2 * g + h], ga = sg4[2 * g + h];
+                const uint32_t u[4] = {ua.x, ua.y, ua.z, ua.w};
+                const uint32_t m[4] = {ga.x, ga.y, ga.z, ga.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    x[4 * h + q] = ((m[q] >> lane) & 1u) ? msigma[row_base(u[q]) + lane] : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++) acc += x[q];
         }
         __syncwarp();
     }
@@ -402,14 +385,14 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
 // Pull into up to 32 light vertices at once, one per lane (pivots ns_l; 0:
 // none), edge-parallel over the concatenation of their in-adjacency lists:
 // lane e finds its vertex by a binary search over the inclusive degree prefix
-// held across the lanes.  Positions arrive grouped by vertex; the running sums
-// are written out whenever the vertex changes.  Returns the discovered mask of
-// the lane's own vertex.
+// held across the lanes.  Positions arrive grouped by vertex, so one running
+// sum per lane (pivot) is written out whenever the vertex changes.  Returns the
+// discovered mask of the lane's own vertex.
 __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, uint32_t ns_l,
                                                  const uint32_t *__restrict__ fprev, uint32_t *msigma,
                                                  uint32_t *su, uint32_t *sg, uint32_t *sk)
 {
-    const unsigned lane = lane_id(), g = lane >> 3, j = lane & 7u;
+    const unsigned lane = lane_id();
     uint32_t b = 0, d = 0;
     if (ns_l) {
         b = rv.col[u_l];
@@ -423,28 +406,8 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
     }
     const uint32_t total = __shfl_sync(FULL_MASK, inc, 31);
     const uint32_t shift = b - (inc - d);  // position of concatenated index e: shift_k + e
-    uint32_t mine = 0, fpart = 0;
-    uint4 acc = make_uint4(0, 0, 0, 0);
+    uint32_t mine = 0, acc = 0, fo = 0;
     int cur = -1;
-    // write the sums of vertex `cur` (pivots found) and reset
-    auto flush = [&]() {
-        const uint4 t = quad_total(acc);
-        uint32_t fo = fpart;
-        fo |= __shfl_xor_sync(FULL_MASK, fo, 8);
-        fo |= __shfl_xor_sync(FULL_MASK, fo, 16);
-        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
-        if (g == 0) {
-            uint32_t *row = msigma + row_base(uc) + 4 * j;
-            const uint32_t nib = (fo >> (4 * j)) & 0xFu;
-            if (nib & 1u) row[0] = t.x;
-            if (nib & 2u) row[1] = t.y;
-            if (nib & 4u) row[2] = t.z;
-            if (nib & 8u) row[3] = t.w;
-        }
-        if ((int)lane == cur) mine = fo;
-        acc = make_uint4(0, 0, 0, 0);
-        fpart = 0;
-    };
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t e = base + lane;
         uint32_t k = 0;
@@ -464,38 +427,66 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
         sg[lane] = fm;
         sk[lane] = k;
         __syncwarp();
+        const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
+        const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
 #pragma unroll 1
-        for (int g8 = 0; g8 < 4; g8++) {
-            if (!((act >> (8 * g8)) & 0xffu)) continue;
-            const int k0 = (int)sk[8 * g8], k7 = (int)sk[8 * g8 + 7];
+        for (int g = 0; g < 4; g++) {
+            if (!((act >> (8 * g)) & 0xffu)) continue;
+            uint32_t x[8], mor = 0;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint4 uu = su4[2 * g + h], mm = sg4[2 * g + h];
+                const uint32_t u4[4] = {uu.x, uu.y, uu.z, uu.w};
+                const uint32_t m4[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    x[4 * h + q] = ((m4[q] >> lane) & 1u) ? msigma[row_base(u4[q]) + lane] : 0u;
+                    mor |= m4[q];
+                }
+            }
+            const int k0 = (int)sk[8 * g], k7 = (int)sk[8 * g + 7];
             if (k0 == k7) {
                 // all eight positions belong to one vertex (k is nondecreasing)
                 if (k0 != cur) {
-                    if (cur >= 0) flush();
+                    if (cur >= 0) {
+                        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+                        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
+                        if ((int)lane == cur) mine = fo;
+                    }
                     cur = k0;
+                    acc = 0;
+                    fo = 0;
                 }
-                const uint32_t m0 = sg[8 * g8 + g], m1 = sg[8 * g8 + g + 4];
-                quad_add(acc, msigma, su[8 * g8 + g], m0, j);
-                quad_add(acc, msigma, su[8 * g8 + g + 4], m1, j);
-                fpart |= m0 | m1;
+                acc += ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
+                fo |= mor;
                 continue;
             }
-#pragma unroll 1
+#pragma unroll
             for (int q = 0; q < 8; q++) {
-                const uint32_t m = sg[8 * g8 + q];
+                const uint32_t m = sg[8 * g + q];
                 if (!m) continue;
-                const int kq = (int)sk[8 * g8 + q];
+                const int kq = (int)sk[8 * g + q];
                 if (kq != cur) {
-                    if (cur >= 0) flush();
+                    if (cur >= 0) {
+                        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+                        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
+                        if ((int)lane == cur) mine = fo;
+                    }
                     cur = kq;
+                    acc = 0;
+                    fo = 0;
                 }
-                if (g == 0) quad_add(acc, msigma, su[8 * g8 + q], m, j);
-                fpart |= m;
+                acc += x[q];
+                fo |= m;
             }
         }
         __syncwarp();
     }
-    if (cur >= 0) flush();
+    if (cur >= 0) {
+        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
+        if ((int)lane == cur) mine = fo;
+    }
     return mine;
 }
 
@@ -516,18 +507,10 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
             const uint32_t ns = srcmask & ~seen[u];
             if (!ns) continue;
             const uint32_t b0 = rv.col[u] + rv.hitem_k[t] * AXBC_SPAN;
-            uint4 acc;
+            uint32_t acc;
             const uint32_t nm =
                 pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg, acc);
-            const uint4 tot = quad_total(acc);
-            if (lane < 8) {
-                uint32_t *row = msigma + row_base(u) + 4 * lane;
-                const uint32_t nib = (nm >> (4 * lane)) & 0xFu;
-                if (nib & 1u) atomicAdd(row + 0, tot.x);
-                if (nib & 2u) atomicAdd(row + 1, tot.y);
-                if (nib & 4u) atomicAdd(row + 2, tot.z);
-                if (nib & 8u) atomicAdd(row + 3, tot.w);
-            }
+            if ((nm >> lane) & 1u) atomicAdd(&msigma[row_base(u) + lane], acc);
             bool first = false;
             if (lane == 0 && nm) first = atomicOr(&fcur[u], nm) == 0u;
             list_append(ll, L, first, u);
