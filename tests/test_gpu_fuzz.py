@@ -32,7 +32,7 @@ def random_graph(rng):
     return e.astype(np.uint64), n
 
 
-@pytest.mark.parametrize("case", range(100))
+@pytest.mark.parametrize("case", range(200))
 def test_random_sampled_runs(axbc, orc, case):
     rng = np.random.default_rng(1000 + case)
     e, n = random_graph(rng)
