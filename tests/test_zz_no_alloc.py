@@ -61,3 +61,35 @@ def test_static_pivot_rejects_oversized_graph(axbc):
                                 1.0, 0, C.addressof(fbuf), None, None)
     assert rc == 5  # AXBC_ERR_RANGE, refused before any device work
     assert b"at most" in L.axbc_last_error()
+
+
+@pytest.mark.parametrize("case", range(20))
+def test_static_pivot_on_random_graphs(axbc, orc, case):
+    """Random multigraphs (directed or not, with or without the one-degree
+    reduction) against the oracle, several pivots accumulating in one bc."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(500 + case)
+    n = int(rng.integers(2, 3000))
+    e = rng.integers(0, n, size=(int(rng.integers(0, 8 * n)), 2)).astype(np.uint64)
+    undirected = bool(rng.random() < 0.7)
+    H = int(rng.random() < 0.4) if undirected else 0
+    g = orc.pipeline(e, n, undirected, H)
+    col = _dev(torch, g.col, np.int32)
+    row = _dev(torch, g.row if g.m else np.zeros(1, np.uint32), np.int32)
+    reach = _dev(torch, g.reach, np.int32) if H else None
+    bc = torch.zeros(n, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    L = axbc.lib()
+    piv = rng.integers(0, n, size=5).astype(np.uint32)
+    p = rng.random(5) * 0.5 + 1e-3
+    for v0, pp in zip(piv, p):
+        st = axbc.PivotStats()
+        rc = L.axbc_bc_pivot_static(col.data_ptr(), row.data_ptr(),
+                                    None if reach is None else reach.data_ptr(),
+                                    n, g.m, int(v0), float(pp), H, bc.data_ptr(), None,
+                                    C.byref(st))
+        assert rc == 0, L.axbc_last_error().decode()
+    want, _, _ = orc.bc_pivots(g, piv, p, H)
+    got = bc.cpu().numpy()
+    same = (got == want) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), f"case {case}: n={n} m={g.m} H={H}: {np.count_nonzero(~same)} differ"
