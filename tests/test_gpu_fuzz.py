@@ -56,3 +56,32 @@ def test_random_sampled_runs(axbc, orc, case):
         assert got[k] == want[k], (what, k)
     same_bits(ctx.bc(), want["bc"], what)
     same_bits(ctx.delta(), want["delta_last"], what + " (last delta)")
+
+
+@pytest.mark.parametrize("case", range(40))
+def test_random_plain_and_batch_passes(axbc, orc, case):
+    """The plain one-pivot pass and the batched pass on random multigraphs,
+    with random direction-switch factors, against the oracle's pivot list."""
+    rng = np.random.default_rng(5000 + case)
+    e, n = random_graph(rng)
+    undirected = bool(rng.random() < 0.7)
+    H = int(rng.random() < 0.4) if undirected else 0
+    g = orc.pipeline(e, n, undirected, H)
+    G = axbc.Graph.from_csc(g.col, g.row, g.reach)
+    ctx = axbc.Context(G)
+    f_plain, f_batch = (float(x) for x in rng.choice([0.0, 0.125, 1.0, 8.0, 1e30], size=2))
+    ctx.set_tuning(f_plain, f_batch)
+    k = int(rng.integers(1, 33))
+    piv = rng.integers(0, n, size=k).astype(np.uint32)
+    p = rng.random(k) + 1e-3
+    want, dl, te = orc.bc_pivots(g, piv, p, H)
+    what = f"case {case}: n={n} m={g.m} undirected={undirected} H={H} k={k} f={f_plain},{f_batch}"
+    for v, pp in zip(piv[:6], p[:6]):
+        ctx.run_pivot(int(v), float(pp), H)
+    want6, _, _ = orc.bc_pivots(g, piv[:6], p[:6], H)
+    same_bits(ctx.bc(), want6, what + " (plain)")
+    ctx.reset()
+    st = ctx.run_batch(piv, p, H)
+    assert sum(s["te"] for s in st) == te, what
+    same_bits(ctx.bc(), want, what + " (batch)")
+    same_bits(ctx.delta(), dl, what + " (batch, last delta)")
