@@ -1193,9 +1193,13 @@ static LevelLists lists_of(const axbc_ctx *c)
     return LevelLists{c->lpool, c->lstart, c->lcount, c->lcap, c->lheavy};
 }
 
+// Largest stored level list: n/8 vertices, or n/2 when no vertex has more than
+// 64 neighbours (a list unit then carries little work whatever it holds, and a
+// wide level of a high-diameter graph is still cheaper to walk than to scan).
 static uint32_t list_max_of(const axbc_ctx *c)
 {
-    return (uint32_t)std::max<uint64_t>(64, c->g->n / 8);
+    const uint64_t n = c->g->n;
+    return (uint32_t)std::max<uint64_t>(64, c->g->max_deg <= 64 ? n / 2 : n / 8);
 }
 
 // Level masks 0..levels-1 exist, and their pointers are in the device table.
