@@ -177,3 +177,51 @@ def test_run_heuristics_terminate(orc, z):
     assert r["nrounds"] > 0
     assert np.all(np.isfinite(r["probs"])) and np.all(r["probs"] > 0)
     assert len(set(r["pivots"].tolist())) == r["nrounds"]
+
+
+def _bfs_counts(col, row, n, src):
+    """Levels and exact (unbounded) shortest-path counts from src over the CSC
+    adjacency (column c lists its neighbours), in plain Python integers."""
+    lvl = [-1] * n
+    sig = [0] * n
+    lvl[src] = 0
+    sig[src] = 1
+    frontier = [src]
+    while frontier:
+        nxt = []
+        for v in frontier:
+            for e in range(col[v], col[v + 1]):
+                u = int(row[e])
+                if lvl[u] == -1:
+                    lvl[u] = lvl[v] + 1
+                    nxt.append(u)
+                if lvl[u] == lvl[v] + 1:
+                    sig[u] += sig[v]
+        frontier = nxt
+    return lvl, sig
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_sigma_against_unbounded_counts(orc, seed):
+    """Self-consistency: the oracle's uint32 path counts equal exact counts
+    reduced mod 2^32, on random graphs (no wrap) and on a grid whose counts
+    exceed 2^32 (binomial coefficients)."""
+    rng = np.random.default_rng(seed)
+    if seed < 4:
+        n = int(rng.integers(5, 300))
+        e = rng.integers(0, n, size=(int(rng.integers(n, 5 * n)), 2)).astype(np.uint64)
+    else:
+        side = 40
+        n = side * side
+        e = np.array([(r * side + c, r * side + c + 1) for r in range(side) for c in range(side - 1)] +
+                     [(r * side + c, (r + 1) * side + c) for r in range(side - 1) for c in range(side)],
+                     np.uint64)
+    g = orc.pipeline(e, n, True, 0)
+    srcs = [0] if seed >= 4 else rng.integers(0, n, size=3).tolist()
+    for s in srcs:
+        lvl, sig = _bfs_counts(g.col, g.row, n, int(s))
+        _, olvl, osig, _, _ = orc.bc_pivot(g, int(s), 1.0 / n)
+        assert list(olvl) == lvl
+        assert [int(x) for x in osig] == [c % (1 << 32) for c in sig]
+        if seed >= 4:
+            assert max(sig) > (1 << 32)  # the grid's counts wrap
