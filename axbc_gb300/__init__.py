@@ -82,6 +82,11 @@ _SIGS = {
                                            C.POINTER(_P)]),
     "axbc_graph_generate_grid": (C.c_int, [C.c_uint32, C.c_double, C.c_double, C.c_uint64,
                                            C.POINTER(_P)]),
+    "axbc_graph_from_edges": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_int, C.c_int,
+                                        C.POINTER(_P)]),
+    "axbc_kron_edges": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_uint64, _P, C.c_int, _P]),
+    "axbc_graph_generate_kronecker": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.c_uint64, _P,
+                                                C.c_int, C.POINTER(_P)]),
     "axbc_graph_destroy": (C.c_int, [_P]),
     "axbc_graph_info": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                   C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
@@ -208,6 +213,17 @@ def read_edge_file(path, n):
     return arr.reshape(-1, 2)
 
 
+def kron_edges(scale, edgefactor=16, seed1=23, seed2=24, stage=2, initiator=None):
+    """The Graph500 generator's edge list, generated on the device, as int64
+    (source, target) pairs: stage 2 = make_graph's output, 1 = before the edge
+    scramble, 0 = before the vertex permutation."""
+    out = np.empty(2 * (1 << scale) * edgefactor, np.int64)
+    ini = None if initiator is None else (C.c_double * 4)(*initiator)
+    _check(lib().axbc_kron_edges(scale, edgefactor, seed1, seed2,
+                                 C.cast(ini, _P) if ini is not None else None, stage, _ptr(out)))
+    return out.reshape(-1, 2)
+
+
 class Graph:
     """A graph resident on the current CUDA device (reference CSC layout)."""
 
@@ -232,6 +248,27 @@ class Graph:
         h = _P()
         _check(lib().axbc_graph_generate_rmat(scale, edgefactor, seed, int(directed), H,
                                               C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_edges(cls, edges, n, undirected=True, H=0):
+        """Device ingest of an edge list (mirror, norm_graph, one-degree
+        reduction, build_csc; src/axbc2d.c:333-351, 695-907)."""
+        e = np.ascontiguousarray(np.asarray(edges, np.uint64).reshape(-1, 2))
+        h = _P()
+        _check(lib().axbc_graph_from_edges(_ptr(e) if len(e) else None, len(e), n, int(undirected), H,
+                                           C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def kronecker(cls, scale, edgefactor=16, seed1=23, seed2=24, H=0, initiator=None):
+        """The reference's synthetic graph: the Graph500 generator's edges
+        (gen_graph, src/axbc2d.c:518-527), generated and built on the device."""
+        h = _P()
+        ini = None if initiator is None else (C.c_double * 4)(*initiator)
+        _check(lib().axbc_graph_generate_kronecker(scale, edgefactor, seed1, seed2,
+                                                   C.cast(ini, _P) if ini is not None else None,
+                                                   H, C.byref(h)))
         return cls(h)
 
     @classmethod

@@ -25,7 +25,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-Xcompiler", "-Wno-unused-function", "-I", os.path.join(ROOT, "include")]
 LIB_SOURCES = ["api.cu", "graph.cu", "single.cu", "batch.cu", "sampler.cu", "serve.cu", "compat.cu",
-               "tune.cu", "noalloc.cu", "host_graph.cpp"]
+               "tune.cu", "noalloc.cu", "kron.cu", "host_graph.cpp"]
+# the Graph500 generator's binomial draws round every product and sum apart,
+# as the host code they restate does
+FILE_FLAGS = {"kron.cu": ["-fmad=false"]}
 CLI_SOURCES = ["cli.cpp"]
 
 
@@ -55,7 +58,7 @@ def _compile(src: str, force: bool, verbose: bool) -> str:
     deps = [src] + _headers()
     if not force and not _stale(out, deps):
         return out
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", out]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", out]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "c++", *NVCC_FLAGS, "-c", src, "-o", out]
     if verbose:

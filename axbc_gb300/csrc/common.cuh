@@ -260,6 +260,14 @@ struct axbc_ctx {
     int bwd_blocks_per_sm = 0;  // resident blocks of the backward kernel
 };
 
+// graph.cu: sort adjacency keys ((column << 32) | row, all-ones = none), drop
+// duplicates and self-loops (norm_graph), optionally reduce degree-1
+// vertices, and build the graph; kron.cu: the Graph500 generator's edges on the
+// device as (source << 32 | target), stage 0 split, 1 permuted, 2 scrambled
+int axbc_keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetric, int H, axbc_graph **out);
+int axbc_kron_device(int scale, int edgefactor, uint64_t seed1, uint64_t seed2, const double *initiator,
+                     int stage, uint64_t **d_edges, uint64_t *m_out);
+
 // allocation with byte accounting
 int axbc_dalloc(void **p, size_t bytes, uint64_t *acct);
 void axbc_dfree(void *p);

@@ -419,13 +419,66 @@ __global__ void k_min_uv(const uint64_t *__restrict__ keys, uint64_t nk, unsigne
     atomicMin(out, best);
 }
 
-// Sort device keys, dedupe, build the CSC on the device and wrap it in a graph.
-// H == 1 runs the one-degree reduction on the host.
-int axbc_edges_to_csc_host_H1(const uint64_t *sorted_uv, uint64_t ned, uint64_t n,
-                              std::vector<uint32_t> &col, std::vector<uint32_t> &row,
-                              std::vector<uint32_t> &reach);
+// One-degree reduction of a sorted, duplicate-free symmetric list on the device
+// (degree_reduction, src/axbc2d.c:695-807).  Entry i is the pair (a, b) = (key
+// >> 32, key & 0xffffffff); the list is ordered by (a, b), the order the
+// reference sorts (u, v) pairs in, because the pair set is symmetric.
+//   - entry i is a leaf entry when a != b and it is the only entry of a;
+//   - entries that are neither leaf entries nor self-loops form the kept list;
+//     a kept entry (x, y) is dropped when y is a leaf vertex: the reference's
+//     merge of the removed pairs (y's neighbour, y) against the kept list
+//     finds exactly these, since every such pair is in the kept list;
+//   - reach[x] counts the removed pairs (x, leaf) that the merge consumed:
+//     those with x <= the first vertex of the last kept entry (none when the
+//     kept list is empty).
+__global__ void k_leaf_entries(const uint64_t *__restrict__ keys, uint64_t m, uint8_t *__restrict__ leafv,
+                               uint8_t *__restrict__ kind, unsigned long long *__restrict__ last_kept)
+{
+    unsigned long long best = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        const uint32_t a = (uint32_t)(k >> 32), b = (uint32_t)k;
+        const bool alone = (i == 0 || (uint32_t)(keys[i - 1] >> 32) != a) &&
+                           (i + 1 == m || (uint32_t)(keys[i + 1] >> 32) != a);
+        uint8_t t;
+        if (a == b) {
+            t = 0;  // self-loop: dropped
+        } else if (alone) {
+            t = 1;  // leaf entry
+            leafv[a] = 1;
+        } else {
+            t = 2;  // kept entry
+            best = best > i + 1 ? best : i + 1;
+        }
+        kind[i] = t;
+    }
+    atomicMax(last_kept, best);
+}
 
-static int keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetric, int H,
+__global__ void k_leaf_reduce(const uint64_t *__restrict__ keys, uint64_t m, const uint8_t *__restrict__ leafv,
+                              uint8_t *__restrict__ kind, uint32_t *__restrict__ reach,
+                              const unsigned long long *__restrict__ last_kept)
+{
+    const unsigned long long lk = *last_kept;  // 1 + index of the last kept entry, 0 if none
+    const uint32_t amax = lk ? (uint32_t)(keys[lk - 1] >> 32) : 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        const uint32_t b = (uint32_t)k;
+        if (kind[i] == 1) {
+            if (lk && b <= amax) atomicAdd(&reach[b], 1u);
+            kind[i] = 0;
+        } else if (kind[i] == 2) {
+            kind[i] = leafv[b] ? 0 : 1;
+        }
+    }
+}
+
+// Sort device keys, dedupe, reduce degree-1 vertices (H == 1), build the CSC
+// and wrap it in a graph.
+
+int axbc_keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetric, int H,
                          axbc_graph **out)
 {
     cudaStream_t s = 0;
@@ -477,24 +530,45 @@ static int keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetri
         return AXBC_ERR_RANGE;
     }
 
-    if (H == 1) {
-        // host one-degree reduction on the (u,v)-sorted edge list; for a
-        // symmetric edge set the (column,row)-sorted keys read as (u,v) pairs
-        // are that list
-        std::vector<uint64_t> h(m);
-        CU(cudaMemcpy(h.data(), d_keys, m * 8, cudaMemcpyDeviceToHost));
-        std::vector<uint64_t> uv(2 * m);
-        for (uint64_t i = 0; i < m; i++) {
-            uv[2 * i] = h[i] >> 32;
-            uv[2 * i + 1] = (uint32_t)h[i];
-        }
+    std::vector<uint32_t> reach;
+    if (H == 1 && m > 0) {
         if (!symmetric) {
             axbc_set_error("one-degree reduction of a generated graph needs a symmetric graph");
             return AXBC_ERR_INVALID;
         }
-        std::vector<uint32_t> col, row, reach;
-        TRY(axbc_edges_to_csc_host_H1(uv.data(), m, n, col, row, reach));
-        return graph_from_host(col.data(), row.data(), n, row.size(), reach.data(), 1, out);
+        uint8_t *d_leafv = nullptr, *d_kind = nullptr;
+        uint32_t *d_reach = nullptr;
+        unsigned long long *d_last = nullptr;
+        TRY(axbc_dalloc((void **)&d_leafv, n, nullptr));
+        TRY(axbc_dalloc((void **)&d_kind, m, nullptr));
+        TRY(axbc_dalloc((void **)&d_reach, n * 4, nullptr));
+        TRY(axbc_dalloc((void **)&d_last, 8, nullptr));
+        CU(cudaMemset(d_leafv, 0, n));
+        CU(cudaMemset(d_reach, 0, n * 4));
+        CU(cudaMemset(d_last, 0, 8));
+        k_leaf_entries<<<2048, 256>>>(d_keys, m, d_leafv, d_kind, d_last);
+        CU_LAUNCH("k_leaf_entries");
+        k_leaf_reduce<<<2048, 256>>>(d_keys, m, d_leafv, d_kind, d_reach, d_last);
+        CU_LAUNCH("k_leaf_reduce");
+        uint64_t *d_kept = nullptr;
+        TRY(axbc_dalloc((void **)&d_kept, m * 8, nullptr));
+        TRY(axbc_dalloc((void **)&d_nsel, 8, nullptr));
+        tmp_bytes = 0;
+        cub::DeviceSelect::Flagged(nullptr, tmp_bytes, d_keys, d_kind, d_kept, d_nsel, (int64_t)m, s);
+        TRY(axbc_dalloc(&d_tmp, tmp_bytes, nullptr));
+        cub::DeviceSelect::Flagged(d_tmp, tmp_bytes, d_keys, d_kind, d_kept, d_nsel, (int64_t)m, s);
+        CU_LAUNCH("select kept entries");
+        CU(cudaMemcpy(&m, d_nsel, 8, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(d_keys, d_kept, m * 8, cudaMemcpyDeviceToDevice));
+        reach.resize(n);
+        CU(cudaMemcpy(reach.data(), d_reach, n * 4, cudaMemcpyDeviceToHost));
+        axbc_dfree(d_tmp);
+        axbc_dfree(d_nsel);
+        axbc_dfree(d_kept);
+        axbc_dfree(d_last);
+        axbc_dfree(d_reach);
+        axbc_dfree(d_kind);
+        axbc_dfree(d_leafv);
     }
 
     uint32_t *d_row = nullptr, *d_cnt = nullptr;
@@ -511,7 +585,68 @@ static int keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetri
     CU(cudaMemcpy(row.data(), d_row, m * 4, cudaMemcpyDeviceToHost));
     axbc_dfree(d_row);
     axbc_dfree(d_cnt);
-    return graph_from_host(col.data(), row.data(), n, m, nullptr, symmetric, out);
+    return graph_from_host(col.data(), row.data(), n, m, reach.empty() ? nullptr : reach.data(), symmetric, out);
+}
+
+// adjacency keys of a host edge list: (u,v) and, when mirrored and u != v, (v,u)
+__global__ void k_list_to_keys(const uint64_t *__restrict__ edges, uint64_t ne, uint64_t n, int mirror,
+                               uint64_t *__restrict__ keys, int *__restrict__ bad)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ne;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t u = edges[2 * i], v = edges[2 * i + 1];
+        if (u >= n || v >= n) {
+            atomicExch(bad, 1);
+            keys[(mirror ? 2 : 1) * i] = ~0ull;
+            if (mirror) keys[2 * i + 1] = ~0ull;
+            continue;
+        }
+        if (mirror) {
+            keys[2 * i] = ckey((uint32_t)u, (uint32_t)v);
+            keys[2 * i + 1] = u == v ? ~0ull : ckey((uint32_t)v, (uint32_t)u);
+        } else {
+            keys[i] = ckey((uint32_t)u, (uint32_t)v);
+        }
+    }
+}
+
+extern "C" int axbc_graph_from_edges(const uint64_t *edges, uint64_t nedges, uint64_t n, int undirected,
+                                     int H, axbc_graph **g)
+{
+    CHECK_ARG(g && (edges || nedges == 0), "axbc_graph_from_edges: null argument");
+    CHECK_ARG(n > 0 && n < 0xffffffffull, "axbc_graph_from_edges: n must be in [1, 2^32-1)");
+    CHECK_ARG(H == 0 || H == 1, "axbc_graph_from_edges: H must be 0 or 1");
+    CHECK_ARG(!(H == 1 && !undirected),
+              "axbc_graph_from_edges: the one-degree reduction runs on undirected graphs here "
+              "(axbc_edges_to_csc takes directed ones)");
+    const uint64_t nk = undirected ? 2 * nedges : nedges;
+    uint64_t *d_edges = nullptr, *d_keys = nullptr;
+    int *d_bad = nullptr;
+    int rc = AXBC_OK;
+    if (nk == 0) return graph_from_host(std::vector<uint32_t>(n + 1, 0).data(), nullptr, n, 0, nullptr, 1, g);
+    TRY(axbc_dalloc((void **)&d_bad, sizeof(int), nullptr));
+    rc = axbc_dalloc((void **)&d_edges, nedges * 16, nullptr);
+    if (!rc) rc = axbc_dalloc((void **)&d_keys, nk * 8, nullptr);
+    if (!rc) {
+        int bad = 0;
+        if (cudaMemset(d_bad, 0, sizeof(int)) != cudaSuccess ||
+            cudaMemcpy(d_edges, edges, nedges * 16, cudaMemcpyHostToDevice) != cudaSuccess) {
+            rc = axbc_cuda_fail(cudaGetLastError(), "edge upload", __FILE__, __LINE__);
+        } else {
+            k_list_to_keys<<<2048, 256>>>(d_edges, nedges, n, undirected, d_keys, d_bad);
+            if (cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = axbc_cuda_fail(cudaGetLastError(), "k_list_to_keys", __FILE__, __LINE__);
+            else if (bad) {
+                axbc_set_error("axbc_graph_from_edges: an edge has a vertex >= n");
+                rc = AXBC_ERR_INVALID;
+            }
+        }
+    }
+    axbc_dfree(d_edges);
+    axbc_dfree(d_bad);
+    if (!rc) rc = axbc_keys_to_graph(d_keys, nk, n, undirected, H, g);
+    axbc_dfree(d_keys);
+    return rc;
 }
 
 extern "C" int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed, int directed,
@@ -527,7 +662,7 @@ extern "C" int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed
     TRY(axbc_dalloc((void **)&d_keys, 2 * ne * 8, nullptr));
     k_rmat<<<4096, 256>>>(ne, scale, seed, directed, d_keys, nullptr);
     CU_LAUNCH("k_rmat");
-    int rc = keys_to_graph(d_keys, 2 * ne, n, !directed, H, g);
+    int rc = axbc_keys_to_graph(d_keys, 2 * ne, n, !directed, H, g);
     axbc_dfree(d_keys);
     return rc;
 }
@@ -556,7 +691,7 @@ extern "C" int axbc_graph_generate_grid(uint32_t side, double drop_prob, double 
     if (lr > lr_cap) lr = lr_cap;
     if (lr) k_longrange<<<256, 256>>>(lr, n, seed, d_keys + 2 * ntot);
     CU_LAUNCH("k_longrange");
-    int rc = keys_to_graph(d_keys, 2 * ntot + 2 * lr, n, 1, 0, g);
+    int rc = axbc_keys_to_graph(d_keys, 2 * ntot + 2 * lr, n, 1, 0, g);
     axbc_dfree(d_keys);
     axbc_dfree(d_kept);
     return rc;

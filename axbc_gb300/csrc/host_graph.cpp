@@ -100,25 +100,6 @@ T *copy_out(const std::vector<T> &v)
 
 }  // namespace
 
-// H == 1 tail of the pipeline on a list already sorted and deduplicated by
-// norm_graph (used by the device generators).
-int axbc_edges_to_csc_host_H1(const uint64_t *sorted_uv, uint64_t ned, uint64_t n,
-                              std::vector<uint32_t> &col, std::vector<uint32_t> &row,
-                              std::vector<uint32_t> &reach)
-{
-    std::vector<Edge> e(ned);
-    for (uint64_t i = 0; i < ned; i++) e[i] = {sorted_uv[2 * i], sorted_uv[2 * i + 1]};
-    reach.assign(n, 0);
-    degree_reduce(e, reach);
-    norm(e);
-    if (e.size() >= 0xffffffffull) {
-        axbc_set_error("too many adjacency entries for 32-bit offsets");
-        return AXBC_ERR_RANGE;
-    }
-    csc(e, n, col, row);
-    return AXBC_OK;
-}
-
 extern "C" int axbc_edges_to_csc(const uint64_t *edges, uint64_t nedges, uint64_t n,
                                  int undirected, int H, uint32_t **col, uint32_t **row,
                                  uint64_t *m, uint32_t **reach, uint64_t *removed_leaves)

@@ -1,10 +1,12 @@
 """Run multi-source batches on a generated graph and print per-batch statistics.
 
     python -m axbc_gb300.runbatch --graph grid:1024 [--batches 1] [--width 32] [--seed 7]
-    python -m axbc_gb300.runbatch --graph rmat:21 [--edgefactor 16] ...
+    python -m axbc_gb300.runbatch --graph kron:21 [--edgefactor 16] ...
 
 Graphs: `grid:SIDE` (SIDE x SIDE four-neighbour grid, 2% of edges dropped,
-0.01% long-range edges, seed 7) or `rmat:SCALE` (R-MAT, undirected).  Pivots
+0.01% long-range edges, seed 7), `kron:SCALE` (the Graph500 generator with
+the reference's seeds 23/24, undirected) or `rmat:SCALE` (the library's R-MAT
+generator, undirected).  Pivots
 are drawn uniformly among vertices of nonzero degree with p = 1/n.  One JSON
 line per batch: wall time, levels, traversed edges, per-kind kernel times and
 how many levels overflowed their vertex list.  Meant for profiling one kernel
@@ -32,6 +34,8 @@ def main():
     kind, size = a.graph.split(":")
     if kind == "grid":
         G = ax.Graph.grid(int(size), 0.02, 1e-4, seed=7)
+    elif kind == "kron":
+        G = ax.Graph.kronecker(int(size), a.edgefactor, 23, 24)
     elif kind == "rmat":
         G = ax.Graph.rmat(int(size), a.edgefactor, seed=23)
     else:

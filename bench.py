@@ -178,10 +178,10 @@ def serve_bench(args):
     import torch
     import axbc_gb300 as ax
     torch.cuda.init()
-    graphs = [("kronecker-s16", ax.Graph.rmat(16, 16, seed=16)),
-              ("kronecker-s18", ax.Graph.rmat(18, 16, seed=18)),
-              ("kronecker-s20", ax.Graph.rmat(20, 16, seed=20)),
-              ("kronecker-s22", ax.Graph.rmat(22, 16, seed=22)),
+    graphs = [("kronecker-s16", ax.Graph.kronecker(16, 16)),
+              ("kronecker-s18", ax.Graph.kronecker(18, 16)),
+              ("kronecker-s20", ax.Graph.kronecker(20, 16)),
+              ("kronecker-s22", ax.Graph.kronecker(22, 16)),
               ("grid-1024", ax.Graph.grid(1024, 0.02, 1e-4, seed=7))]
     srv = ax.Server()
     gids = [srv.add_graph(G, H=0) for _, G in graphs]
@@ -226,7 +226,7 @@ def serve_bench(args):
            "span_s": span, "passes": st["passes"], "lanes_per_pass": st["lanes"] / max(1, st["passes"]),
            "p50_by_graph_s": {k: float(np.median(v)) for k, v in per_graph.items()},
            "worker_by_graph": {graphs[i][0]: srv.graph_stats(g) for i, g in enumerate(gids)},
-           "dtype": "u32 path counts, f32 dependencies", "data": "synthetic (device R-MAT, grid)",
+           "dtype": "u32 path counts, f32 dependencies", "data": "synthetic (Graph500 generator, seeds 23/24, on the device; grid)",
            "config": {"workload": "serving: resident kronecker s16/s18/s20/s22 ef16 + grid 1024^2; "
                                   "Poisson arrivals (seed 11); -z 0..5; width 8; -N log-uniform "
                                   "64-2048 or -c 1 -x 4..16",
@@ -264,7 +264,12 @@ def main():
     import axbc_gb300 as ax
     ax.lib()
 
-    G = ax.Graph.rmat(args.scale, args.edgefactor, seed=23)
+    # the reference's own input: the Graph500 generator with gen_graph's seeds
+    # (23, 24) and initiator, generated and built on the device (set-up, untimed)
+    t_graph = time.perf_counter()
+    G = ax.Graph.kronecker(args.scale, args.edgefactor, 23, 24)
+    config["graph"] = {"generator": "Graph500 (seeds 23/24, initiator .57/.19/.19/.05)",
+                       "n": G.n, "m": G.m, "build_s": round(time.perf_counter() - t_graph, 3)}
     stream = torch.cuda.Stream()
     ctx = ax.Context(G, stream=stream.cuda_stream)
 
@@ -310,7 +315,8 @@ def main():
         out = {"metric": metric, "value": val, "unit": "TE/s", "n_gpus": 1, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": wall * 1000 / max(args.steps, 1),
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "u32 path counts, f32 dependencies/bc", "data": "synthetic",
+               "dtype": "u32 path counts, f32 dependencies/bc",
+               "data": "synthetic: the Graph500 generator's graph (seeds 23/24), generated on the device",
                "config": config, "impl": "reference",
                "cpu_baseline": {"value": val, "unit": "TE/s", "cores": threads, "kind": "port",
                                 "sample": f"{ks[0]} pivots of the step's pivot list per step, "
@@ -433,7 +439,8 @@ def main():
     out = {"metric": metric, "value": value, "unit": "TE/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000 / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "u32 path counts, f32 dependencies/bc", "data": "synthetic",
+           "dtype": "u32 path counts, f32 dependencies/bc",
+               "data": "synthetic: the Graph500 generator's graph (seeds 23/24), generated on the device",
            "config": config, "e2e": e2e, "roofline": roofline, "clocks": clk,
            "gpu_launches": int(launches), "plain_form": plain,
            "te_per_step": te_all / args.steps, "pivots_applied_per_step": int(last["nrounds"])}

@@ -75,6 +75,16 @@ int axbc_read_edge_file(const char *path, uint64_t n, uint64_t **edges, uint64_t
 int axbc_graph_create(const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
                       const uint32_t *reach, axbc_graph **g);
 
+/* The reference's ingest pipeline on the device: upload a host edge list
+ * (uint64 pairs, vertices < n), mirror it when `undirected` (mirror,
+ * src/axbc2d.c:333-351), sort, drop repeats and self-loops except a self-loop
+ * that sorts first (norm_graph, 818-841), with H == 1 remove degree-1
+ * vertices into reach (degree_reduction + init_bc_1degree, 695-807, 866-876;
+ * undirected graphs only), and build the CSC (build_csc, 883-907).  Same
+ * result as axbc_edges_to_csc + axbc_graph_create. */
+int axbc_graph_from_edges(const uint64_t *edges, uint64_t nedges, uint64_t n, int undirected, int H,
+                          axbc_graph **g);
+
 /* Synthetic inputs generated and built on the device: an R-MAT graph of
  * 2^scale vertices and edgefactor*2^scale generated edges (initiator
  * A,B,C = .57,.19,.19), vertex ids scrambled, self-loops and duplicates
@@ -83,6 +93,22 @@ int axbc_graph_create(const uint32_t *col, const uint32_t *row, uint64_t n, uint
  * src/axbc2d.c:518-527; this generator is the library's own.) */
 int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed, int directed, int H,
                              axbc_graph **g);
+/* The reference's own synthetic input, generated on the device: the Graph500
+ * Kronecker generator's edge list (gen_graph, src/axbc2d.c:518-527, calling
+ * make_graph, generator/make_graph.c:35-105), element for element, for
+ * 2^scale vertices, edgefactor * 2^scale edges, seeds seed1/seed2 (the
+ * reference passes 23 and 24) and a 2x2 initiator (NULL: .57/.19/.19/.05).
+ * At most 10^9 edges.
+ *   axbc_kron_edges: the edges as int64 (source, target) pairs into
+ *     edges_host (2 * edgefactor * 2^scale values).  stage 2 is make_graph's
+ *     output; stage 1 the same edges before the edge scramble; stage 0 before
+ *     the vertex permutation.
+ *   axbc_graph_generate_kronecker: the graph the reference builds from that
+ *     list (mirror, norm_graph, optional one-degree reduction, build_csc). */
+int axbc_kron_edges(int scale, int edgefactor, uint64_t seed1, uint64_t seed2,
+                    const double *initiator, int stage, int64_t *edges_host);
+int axbc_graph_generate_kronecker(int scale, int edgefactor, uint64_t seed1, uint64_t seed2,
+                                  const double *initiator, int H, axbc_graph **g);
 /* side x side 4-neighbour grid; each grid edge dropped with probability
  * drop_prob; floor(longrange_frac * kept_edges) extra random edges; mirrored. */
 int axbc_graph_generate_grid(uint32_t side, double drop_prob, double longrange_frac,

@@ -67,8 +67,8 @@ class RunResult(C.Structure):
 def build(force: bool = False, ref: bool = False) -> None:
     """Compile liboracle.so (and the reference generator shim if asked)."""
     target = os.path.join(_HERE, "liboracle.so")
-    src = os.path.join(_HERE, "oracle.c")
-    if force or not os.path.exists(target) or os.path.getmtime(target) < os.path.getmtime(src):
+    newest = max(os.path.getmtime(os.path.join(_HERE, f)) for f in ("oracle.c", "oracle.h", "kron.c"))
+    if force or not os.path.exists(target) or os.path.getmtime(target) < newest:
         subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
     if ref and os.path.isdir("/root/reference/generator"):
         subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
@@ -99,6 +99,10 @@ def lib():
         L.orc_lrand48_seq.argtypes = [C.c_int64, C.c_int64, P]
         L.orc_run.argtypes = [C.POINTER(Graph), C.POINTER(RunParams), P, P, P, P, C.c_uint64, P,
                               C.POINTER(RunResult)]
+        L.orc_kron_edges.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint64, P, C.c_int, P]
+        L.orc_kron_edges.restype = C.c_int64
+        L.orc_kron_perm_key.argtypes = [C.c_uint64] * 5
+        L.orc_kron_perm_key.restype = C.c_uint64
         _LIB = L
     return _LIB
 
@@ -247,21 +251,43 @@ def run(g: CSC, z=0, nbfs=1, bader_c=1, nchecks=1, H=0, seed=4343543, W=1, order
                 dropped=res.dropped, ui_end=res.ui_end, te=res.te, stopped=bool(res.stopped))
 
 
+GRAPH500_INITIATOR = (.57, .19, .19, .05)
+
+
+def kron_edges(scale, edgef, seed1=23, seed2=24, stage=2, initiator=GRAPH500_INITIATOR):
+    """The Graph500 generator restated in oracle/kron.c, as int64 (src, tgt)
+    pairs.  stage 0: before the vertex permutation; 1: permuted, (min, max)
+    pairs; 2: scrambled (the reference make_graph's output order)."""
+    L = lib()
+    ne = (1 << scale) * edgef
+    out = np.empty(2 * ne, np.int64)
+    ini = (C.c_double * 4)(*initiator)
+    got = L.orc_kron_edges(scale, edgef, seed1, seed2, ini, stage, _ptr(out))
+    if got < 0:
+        raise MemoryError("orc_kron_edges")
+    return out.reshape(-1, 2)
+
+
+def kron_perm_key(seed1, seed2, skip_hi, i, T):
+    return int(lib().orc_kron_perm_key(seed1, seed2, skip_hi, i, T))
+
+
 def ref_kron_available() -> bool:
     return os.path.exists(os.path.join(_HERE, "_ref", "libkron_ref.so"))
 
 
-def ref_kron_edges(scale, edgef, seed1=23, seed2=24):
+def ref_kron_edges(scale, edgef, seed1=23, seed2=24, initiator=GRAPH500_INITIATOR):
     """Edges from the reference's own generator (oracle/_ref), as int64 pairs."""
     global _REF
     if _REF is None:
         _REF = C.CDLL(os.path.join(_HERE, "_ref", "libkron_ref.so"))
-        _REF.ref_kron_edges.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint64,
-                                        C.POINTER(C.c_void_p)]
-        _REF.ref_kron_edges.restype = C.c_int64
+        _REF.ref_kron_edges_ini.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_uint64,
+                                            C.c_void_p, C.POINTER(C.c_void_p)]
+        _REF.ref_kron_edges_ini.restype = C.c_int64
         _REF.ref_kron_free.argtypes = [C.c_void_p]
     out = C.c_void_p()
-    ned = _REF.ref_kron_edges(scale, edgef, seed1, seed2, C.byref(out))
+    ini = (C.c_double * 4)(*initiator)
+    ned = _REF.ref_kron_edges_ini(scale, edgef, seed1, seed2, C.cast(ini, C.c_void_p), C.byref(out))
     arr = np.ctypeslib.as_array(C.cast(out, C.POINTER(C.c_int64)), (2 * ned,)).copy()
     _REF.ref_kron_free(out)
     return arr.reshape(-1, 2)

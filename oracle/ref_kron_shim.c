@@ -18,4 +18,14 @@ int64_t ref_kron_edges(int scale, int edgef, uint64_t seed1, uint64_t seed2, int
     return ned;
 }
 
+/* the same with another initiator */
+int64_t ref_kron_edges_ini(int scale, int edgef, uint64_t seed1, uint64_t seed2, const double ini[4],
+                           int64_t **out)
+{
+    double initiator[4] = {ini[0], ini[1], ini[2], ini[3]};
+    int64_t ned = 0;
+    make_graph(scale, (((int64_t)1) << scale) * edgef, seed1, seed2, initiator, &ned, out);
+    return ned;
+}
+
 void ref_kron_free(void *p) { free(p); }

@@ -5,12 +5,13 @@ oracle/_ref by `make -C oracle ref`) with the arguments of gen_graph
 (src/axbc2d.c:518-527: initiator .57/.19/.19/.05, seeds 23 and 24,
 edgefactor 16) and stores:
   kron_s10_ef16.npz   the scale-10 edge list (uint16 pairs, generator order)
-  kron_summary.json   sha256 of the scale-10/12/14 edge lists and, per scale and
+  kron_summary.json   sha256 of the scale-10..20 edge lists and, per scale and
                       -H 0/1, the CSC size, isolated / degree-1 counts, maximum
                       degree, removed leaves, and sha256 of col/row/reach as
                       built by the reference pipeline (mirror, norm_graph,
                       degree_reduction, build_csc) restated in oracle/.
-Usage: python tests/golden/make_golden.py
+Scale 23 (the headline graph, about 3 minutes of CPU) is added with --s23.
+Usage: python tests/golden/make_golden.py [--s23]
 """
 import hashlib
 import json
@@ -32,8 +33,10 @@ def main():
     oracle.build(ref=True)
     if not oracle.ref_kron_available():
         raise SystemExit("reference generator not built (needs the reference sources)")
-    out = {}
-    for scale in (10, 12, 14):
+    scales = [10, 12, 14, 16, 18, 20] + ([23] if "--s23" in sys.argv else [])
+    path = os.path.join(HERE, "kron_summary.json")
+    out = json.load(open(path)) if os.path.exists(path) else {}
+    for scale in scales:
         e = oracle.ref_kron_edges(scale, 16)
         n = 1 << scale
         ent = {"n": n, "edges": int(len(e)), "edges_sha256": sha(e.astype(np.int64))}
@@ -47,10 +50,10 @@ def main():
                 "col_sha256": sha(g.col), "row_sha256": sha(g.row), "reach_sha256": sha(g.reach),
             }
         out[str(scale)] = ent
-        if scale == 10:
+        if scale == 10 and not os.path.exists(os.path.join(HERE, "kron_s10_ef16.npz")):
             np.savez_compressed(os.path.join(HERE, "kron_s10_ef16.npz"),
                                 edges=e.astype(np.uint16))
-    with open(os.path.join(HERE, "kron_summary.json"), "w") as f:
+    with open(path, "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print(json.dumps({k: v["H0"]["m"] for k, v in out.items()}))
 

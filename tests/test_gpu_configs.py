@@ -28,7 +28,8 @@ def csc_of(orc, G):
 
 @pytest.fixture(scope="module")
 def kron20(axbc, orc):
-    G = axbc.Graph.rmat(20, 16, seed=23, H=1)
+    # the reference's scale-20 input (Graph500 generator, seeds 23/24), -H 1
+    G = axbc.Graph.kronecker(20, 16, H=1)
     return G, csc_of(orc, G)
 
 

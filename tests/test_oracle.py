@@ -225,3 +225,58 @@ def test_oracle_sigma_against_unbounded_counts(orc, seed):
         assert [int(x) for x in osig] == [c % (1 << 32) for c in sig]
         if seed >= 4:
             assert max(sig) > (1 << 32)  # the grid's counts wrap
+
+
+@pytest.mark.parametrize("scale", [10, 12, 14])
+def test_restated_generator_matches_golden(orc, scale):
+    """oracle/kron.c (the Graph500 generator restated) reproduces the
+    reference generator's edge list, order included, at the committed sizes."""
+    ent = json.load(open(os.path.join(GOLDEN, "kron_summary.json")))[str(scale)]
+    e = orc.kron_edges(scale, 16)
+    assert len(e) == ent["edges"]
+    assert sha(e) == ent["edges_sha256"]
+
+
+@pytest.mark.parametrize("scale,edgef,seeds,ini", [
+    (6, 16, (23, 24), (.57, .19, .19, .05)),
+    (9, 4, (1, 2), (.57, .19, .19, .05)),
+    (11, 16, (2**40 + 7, 99), (.45, .15, .15, .25)),
+    (8, 32, (0, 0), (.25, .25, .25, .25)),
+])
+def test_restated_generator_against_reference_build(orc, scale, edgef, seeds, ini):
+    """Other sizes, seeds (including high bits) and initiators: the restated
+    generator against the reference generator compiled here, when it is."""
+    if not orc.ref_kron_available():
+        pytest.skip("reference generator not built on this machine")
+    want = orc.ref_kron_edges(scale, edgef, *seeds, initiator=ini)
+    got = orc.kron_edges(scale, edgef, *seeds, initiator=ini)
+    assert np.array_equal(got, want)
+
+
+def test_restated_generator_stages(orc):
+    """Stage 1 is stage 0 under one vertex permutation, each pair stored as
+    (min, max); stage 2 reorders stage 1."""
+    n = 1 << 12
+    s0 = orc.kron_edges(12, 8, stage=0)
+    s1 = orc.kron_edges(12, 8, stage=1)
+    s2 = orc.kron_edges(12, 8, stage=2)
+    assert (s1[:, 0] <= s1[:, 1]).all()
+    key = lambda e: np.sort(e[:, 0] * (1 << 32) + e[:, 1])
+    assert np.array_equal(key(s1), key(s2))
+    # recover the permutation from self-loops and edges to already-mapped
+    # vertices, then check every edge against it
+    img = -np.ones(n, np.int64)
+    loops = s0[:, 0] == s0[:, 1]
+    img[s0[loops, 0]] = s1[loops, 0]
+    for _ in range(8):
+        for (a, b), (c, d) in zip(s0, s1):
+            if img[a] >= 0 and img[b] < 0:
+                img[b] = d if img[a] == c else c
+            elif img[b] >= 0 and img[a] < 0:
+                img[a] = d if img[b] == c else c
+    ok = (img[s0[:, 0]] >= 0) & (img[s0[:, 1]] >= 0)
+    assert ok.mean() > 0.9
+    a, b = img[s0[ok, 0]], img[s0[ok, 1]]
+    assert np.array_equal(np.minimum(a, b), s1[ok, 0]) and np.array_equal(np.maximum(a, b), s1[ok, 1])
+    mapped = img[img >= 0]
+    assert len(np.unique(mapped)) == len(mapped)
