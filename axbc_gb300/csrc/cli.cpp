@@ -6,7 +6,7 @@
 //
 // Same defaults as the reference: -N 1, -c 1 (adaptive stop on), -x 1,
 // -z 0, -H 0, graphs made undirected unless -U, srand48 seed 4343543.
-// New options: -s SEED (srand48 seed), -W WIDTH (pivots per batch, 1..32;
+// New options: -s SEED (srand48 seed), -W WIDTH (pivots per round, 1..64;
 // 1 reproduces the reference's round sequence).  One GPU: -p must be 1x1;
 // -m (force the 2-D multi-GPU code) is accepted and ignored.
 #include <getopt.h>
@@ -176,8 +176,22 @@ int main(int argc, char **argv)
         axbc_host_free(col);
         axbc_host_free(row);
         axbc_host_free(reach);
+    } else if (undirected) {
+        // gen_graph (src/axbc2d.c:518-527): the Graph500 generator, seeds 23 and 24
+        check(axbc_graph_generate_kronecker(scale, edgef, 23, 24, nullptr, H, &g), "graph generation");
     } else {
-        check(axbc_graph_generate_rmat(scale, edgef, 23, !undirected, H, &g), "graph generation");
+        // -U: the generator's pairs as directed edges, through the host pipeline
+        const uint64_t ne = ((uint64_t)1 << scale) * (uint64_t)edgef;
+        std::vector<int64_t> ed(2 * ne);
+        check(axbc_kron_edges(scale, edgef, 23, 24, nullptr, 2, ed.data()), "graph generation");
+        uint32_t *col, *row, *reach;
+        uint64_t m, removed;
+        check(axbc_edges_to_csc((const uint64_t *)ed.data(), ne, N, 0, H, &col, &row, &m, &reach, &removed),
+              "graph pre-processing");
+        check(axbc_graph_create(col, row, N, m, reach, &g), "graph upload");
+        axbc_host_free(col);
+        axbc_host_free(row);
+        axbc_host_free(reach);
     }
     uint64_t n = 0, m = 0, bytes = 0;
     int sym = 0;
