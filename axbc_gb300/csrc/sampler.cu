@@ -70,50 +70,112 @@ __device__ __forceinline__ double d_01_of(int64_t r) { return __ddiv_rn((double)
 __device__ __forceinline__ double d_uniform01(uint64_t &x) { return d_01_of(d_lrand48(x)); }
 
 // ------------------------------------------------- hierarchical prefix
-__global__ void k_hprefix_local(const float *__restrict__ w, uint64_t n, double *__restrict__ local,
-                                double *__restrict__ bsum, int mode, const SamplerState *ss)
+// The prefix of a float weight vector in double, two-level at both scales so
+// that no chain of dependent double additions is long (double adds are slow
+// on this part and a left-to-right sum of millions of terms cannot run in
+// parallel):
+//  - a block of AXBC_SAMPLE_BLOCK (1024) weights is 32 runs of 32; s = running
+//    sum inside a run, P = running sum of the finished runs' totals,
+//    local[i] = P + s; the block total is P after the last run;
+//  - blocks form groups of 32: L = running sum of block totals inside the
+//    group, G = running sum of the finished groups' totals, csum[b] = G + L.
+// Every sum is left to right; the oracle computes the same values.
+#define HP_WARPS 4
+__device__ __forceinline__ float hp_weight(const float *__restrict__ w, uint64_t i, int mode)
+{
+    const float x = __ldg(w + i);
+    // mode 1: the weight 1/(1+bc) of heuristic 5 (src/axbc2d.c:2025-2058)
+    return mode == 1 ? __fdiv_rn(1.0f, __fadd_rn(1.0f, x)) : x;
+}
+
+// one warp per block: lane l owns run l; the run prefixes are staged in shared
+// memory so the stores of local[] are coalesced
+__global__ void __launch_bounds__(32 * HP_WARPS) k_hprefix_local(const float *__restrict__ w, uint64_t n,
+                                                               double *__restrict__ local,
+                                                               double *__restrict__ bsum, int mode,
+                                                               const SamplerState *ss)
 {
     if (ss && (ss->done || ss->nrounds_snap == 0)) return;
+    __shared__ double sd[HP_WARPS][32 * 33];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
-    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < nb;
-         b += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t e = min((b + 1) * AXBC_SAMPLE_BLOCK, n);
-        double t = 0.0;
-        for (uint64_t i = b * AXBC_SAMPLE_BLOCK; i < e; i++) {
-            float x = w[i];
-            // mode 1: the weight 1/(1+bc) of heuristic 5 (src/axbc2d.c:2025-2058)
-            if (mode == 1) x = __fdiv_rn(1.0f, __fadd_rn(1.0f, x));
-            t = __dadd_rn(t, (double)x);
-            local[i] = t;
+    for (uint64_t b = (uint64_t)blockIdx.x * HP_WARPS + wib; b < nb; b += (uint64_t)gridDim.x * HP_WARPS) {
+        const uint64_t base = b * AXBC_SAMPLE_BLOCK, i0 = base + 32 * (uint64_t)lane;
+        const int cnt = i0 >= n ? 0 : (int)min((uint64_t)32, n - i0);
+        double s = 0.0;
+        for (int k = 0; k < cnt; k++) s = __dadd_rn(s, (double)hp_weight(w, i0 + k, mode));
+        // P before run l; c ends as the block total (absent runs add +0)
+        double c = 0.0, pex = 0.0;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const double t = __shfl_sync(FULL_MASK, s, k);
+            if (lane == k) pex = c;
+            c = __dadd_rn(c, t);
         }
-        bsum[b] = t;
+        double r = 0.0;
+        for (int k = 0; k < cnt; k++) {
+            r = __dadd_rn(r, (double)hp_weight(w, i0 + k, mode));
+            sd[wib][lane * 33 + k] = __dadd_rn(pex, r);
+        }
+        __syncwarp();
+        for (int it = 0; it < 32; it++) {
+            const uint64_t i = base + 32 * (uint64_t)it + lane;
+            if (i < n) local[i] = sd[wib][it * 33 + lane];
+        }
+        __syncwarp();
+        if (lane == 0) bsum[b] = c;
     }
 }
 
-// The running sum of the block totals, left to right (one warp: 32 totals
-// load per step, every lane adds them in order, lane k keeps the k-th sum).
-__global__ void k_hprefix_csum(double *csum, uint64_t nb, const SamplerState *ss)
+// csum holds the block totals on entry and their prefix on exit.  One block of
+// 1024 threads; groups are handled in chunks of 1024.
+__global__ void __launch_bounds__(1024, 1) k_hprefix_csum(double *csum, uint64_t nb, const SamplerState *ss)
 {
     if (ss && (ss->done || ss->nrounds_snap == 0)) return;
-    const unsigned lane = threadIdx.x;
-    double c = 0.0;
-    for (uint64_t base = 0; base < nb; base += 32) {
-        const double x = base + lane < nb ? csum[base + lane] : 0.0;
-        double mine = 0.0;
+    __shared__ double s_G[1024];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint64_t ng = (nb + 31) / 32;
+    double G = 0.0;  // warp 0's running sum of group totals
+    for (uint64_t g0 = 0; g0 < ng; g0 += 1024) {
+        const uint64_t gend = min(ng, g0 + 1024);
+        // in-group running sums, in place
+        for (uint64_t g = g0 + wid; g < gend; g += 32) {
+            const uint64_t b = g * 32 + lane;
+            const double x = b < nb ? csum[b] : 0.0;
+            double c = 0.0, mine = 0.0;
 #pragma unroll
-        for (int k = 0; k < 32; k++) {
-            c = __dadd_rn(c, __shfl_sync(FULL_MASK, x, k));
-            if ((int)lane == k) mine = c;
+            for (int k = 0; k < 32; k++) {
+                c = __dadd_rn(c, __shfl_sync(FULL_MASK, x, k));
+                if (lane == k) mine = c;
+            }
+            if (b < nb) csum[b] = mine;
         }
-        if (base + lane < nb) csum[base + lane] = mine;
+        __syncthreads();
+        // G before each group of the chunk (warp 0)
+        if (wid == 0) {
+            for (uint64_t gb = g0; gb < gend; gb += 32) {
+                const uint64_t g = gb + lane;
+                const double tot = g < gend ? csum[min(g * 32 + 31, nb - 1)] : 0.0;
+#pragma unroll
+                for (int k = 0; k < 32; k++) {
+                    if (lane == k && g < gend) s_G[g - g0] = G;
+                    G = __dadd_rn(G, __shfl_sync(FULL_MASK, tot, k));
+                }
+            }
+        }
+        __syncthreads();
+        for (uint64_t b = g0 * 32 + threadIdx.x; b < min(nb, gend * 32); b += 1024)
+            csum[b] = __dadd_rn(s_G[b / 32 - g0], csum[b]);
+        __syncthreads();
     }
 }
 
 int axbc_hprefix_launch(const float *w, uint64_t n, double *local, double *csum, cudaStream_t s)
 {
     const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
-    k_hprefix_local<<<(unsigned)((nb + 127) / 128), 128, 0, s>>>(w, n, local, csum, 0, nullptr);
-    k_hprefix_csum<<<1, 32, 0, s>>>(csum, nb, nullptr);
+    k_hprefix_local<<<(unsigned)min((uint64_t)65535, (nb + HP_WARPS - 1) / HP_WARPS), 32 * HP_WARPS, 0, s>>>(
+        w, n, local, csum, 0, nullptr);
+    k_hprefix_csum<<<1, 1024, 0, s>>>(csum, nb, nullptr);
     CU_LAUNCH("hprefix");
     return AXBC_OK;
 }
@@ -143,6 +205,40 @@ __device__ uint64_t d_hsearch(const double *local, const double *csum, uint64_t 
         if (local[mid] >= rr) hi = mid;
         else lo = mid + 1;
     }
+    *found = 1;
+    return lo < e ? lo : e - 1;
+}
+
+// The same search run by all SAMPLER_TPB threads of a block together (every
+// thread calls it with the same arguments): each step tests SAMPLER_TPB evenly
+// spaced positions at once and keeps the gap holding the first position >= r,
+// so a search of n entries takes a few steps instead of log2(n) dependent loads.
+#define SAMPLER_TPB 256
+__device__ uint64_t blk_first_ge(const double *a, uint64_t lo, uint64_t hi, double r)
+{
+    while (lo < hi) {
+        const uint64_t step = (hi - lo + SAMPLER_TPB - 1) / SAMPLER_TPB;
+        const uint64_t p = lo + (uint64_t)threadIdx.x * step;
+        const int below = __syncthreads_count(p < hi && !(a[p] >= r));
+        if (below == 0) return lo;
+        const uint64_t nhi = min(hi, lo + (uint64_t)below * step);
+        lo = lo + (uint64_t)(below - 1) * step + 1;
+        hi = nhi;
+    }
+    return hi;
+}
+
+__device__ uint64_t blk_hsearch(const double *local, const double *csum, uint64_t n, double r, int *found)
+{
+    const uint64_t B = AXBC_SAMPLE_BLOCK, nb = (n + B - 1) / B;
+    *found = 0;
+    if (n == 0) return 0;
+    const double tot = csum[nb - 1];
+    if (isnan(tot) || !(tot >= r)) return n - 1;
+    const uint64_t b = blk_first_ge(csum, 0, nb, r);
+    const double rr = __dsub_rn(r, b > 0 ? csum[b - 1] : 0.0);
+    const uint64_t e = min((b + 1) * B, n);
+    const uint64_t lo = blk_first_ge(local, b * B, e, rr);
     *found = 1;
     return lo < e ? lo : e - 1;
 }
@@ -211,6 +307,16 @@ __global__ void k_sampler_init(SamplerState *ss, uint32_t *checks, int64_t seed,
 
 // The draws that take one lrand48 value: the pivot and its probability from
 // the value r, for the effective heuristic k in {0, 2, 3, 4, 5}.
+// COOP: called by every thread of a SAMPLER_TPB block with the same
+// arguments, searching together (blk_hsearch); else one thread searches alone.
+template <bool COOP>
+__device__ __forceinline__ uint64_t hsearch_of(const double *local, const double *csum, uint64_t n, double r,
+                                               int *found)
+{
+    return COOP ? blk_hsearch(local, csum, n, r, found) : d_hsearch(local, csum, n, r, found);
+}
+
+template <bool COOP>
 __device__ void d_map_one(int64_t r, int k, uint64_t N, const SamplerDists &D, bool snap0,
                           double S_bc, double S_d, double S_lcc, uint32_t &v0, double &prob)
 {
@@ -221,21 +327,21 @@ __device__ void d_map_one(int64_t r, int k, uint64_t N, const SamplerDists &D, b
     } else if (k == 2) {
         // LCC (src/axbc2d.c:2919-2937)
         const double rr = __dmul_rn(d_01_of(r), S_lcc);
-        uint64_t h = d_hsearch(D.lcc_local, D.lcc_csum, N, rr, &found);
+        uint64_t h = hsearch_of<COOP>(D.lcc_local, D.lcc_csum, N, rr, &found);
         if (!found) h = N - 1;
         v0 = (uint32_t)h;
         prob = __ddiv_rn((double)D.lcc[v0], S_lcc);
     } else if (k == 4) {
         // delta of the last pivot (src/axbc2d.c:2970-2991)
         const double rr = __dmul_rn(d_01_of(r), S_d);
-        uint64_t h = d_hsearch(D.d_local, D.d_csum, N, rr, &found);
+        uint64_t h = hsearch_of<COOP>(D.d_local, D.d_csum, N, rr, &found);
         if (!found) h = N - 1;
         v0 = (uint32_t)h;
         prob = __ddiv_rn((double)D.delta_last[v0], S_d);
     } else {
         // bc (src/axbc2d.c:2941-2969) or 1/(1+bc) (2995-3022)
         const double rr = __dmul_rn(d_01_of(r), S_bc);
-        uint64_t h = d_hsearch(D.bc_local, D.bc_csum, N, rr, &found);
+        uint64_t h = hsearch_of<COOP>(D.bc_local, D.bc_csum, N, rr, &found);
         if (!found) h = N - 1;
         v0 = (uint32_t)h;
         if (k == 3) prob = __ddiv_rn((double)D.bc[v0], S_bc);
@@ -247,6 +353,7 @@ __device__ void d_map_one(int64_t r, int k, uint64_t N, const SamplerDists &D, b
 // the others): v0 and its probability, the reference's rules of
 // src/axbc2d.c:2873-3051.  snap0: no pivot applied yet (the dynamic heuristics
 // then draw uniformly).
+template <bool COOP>
 __device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, const SamplerDists &D,
                            bool snap0, double S_bc, double S_d, double S_lcc, uint32_t &v0,
                            double &prob)
@@ -268,7 +375,7 @@ __device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, c
         v0 = (uint32_t)h;
         prob = __ddiv_rn((double)D.sdn[v0], (double)D.sum_deg);
     } else {
-        d_map_one(d_lrand48(x), k, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
+        d_map_one<COOP>(d_lrand48(x), k, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
     }
     if (z == 6) {
         // mixture probability (src/axbc2d.c:3026-3051)
@@ -296,7 +403,6 @@ __device__ void d_draw_one(uint64_t &x, uint32_t &dist_mix, int z, uint64_t N, c
 // thread t evaluates the draw t steps ahead (drand48 skip-ahead: x -> A_t x +
 // C_t mod 2^48) and the first acceptable one wins, with the state and the
 // rejection count advanced exactly as the sequential loop would.
-#define SAMPLER_TPB 256
 // rejections in a row before the block searches draws in parallel
 #ifndef AXBC_SAMPLER_STREAK
 #define AXBC_SAMPLER_STREAK 4
@@ -376,7 +482,7 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
                 bool acc = false;
                 if ((uint64_t)t < allow) {
                     const uint64_t xt = (s_A[t + 1] * x + s_C[t + 1]) & 0xFFFFFFFFFFFFULL;
-                    d_map_one((int64_t)(xt >> 17), z, N, D, snap0, S_bc, S_d, S_lcc, v, pr);
+                    d_map_one<false>((int64_t)(xt >> 17), z, N, D, snap0, S_bc, S_d, S_lcc, v, pr);
                     acc = !(v < N && is_used(used, v));
                 }
                 if (lead) s_best = SAMPLER_TPB;
@@ -402,7 +508,7 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
                 __syncthreads();
                 continue;
             }
-            d_draw_one(x, dist_mix, z, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
+            d_draw_one<true>(x, dist_mix, z, N, D, snap0, S_bc, S_d, S_lcc, v0, prob);
             if (v0 < N && is_used(used, v0)) BSM++;
             else good = true;
         }
@@ -692,17 +798,17 @@ int sr_draw(axbc_ctx *c, SampledRun *r)
     const bool dyn_bc = z == 3 || z == 5 || z == 6;
     const bool dyn_d = z == 4 || z == 6;
     const uint64_t nbB = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
-    const unsigned hb = (unsigned)((nbB + 127) / 128);
+    const unsigned hb = (unsigned)min((uint64_t)65535, (nbB + HP_WARPS - 1) / HP_WARPS);
     if (dyn_bc) {
         D.bc_local = r->dyn_local;
         D.bc_csum = r->dyn_csum;
         {
             ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
-            k_hprefix_local<<<hb, 128, 0, s>>>(r->bc, n, r->dyn_local, r->dyn_csum, z == 5 ? 1 : 0, r->ss);
+            k_hprefix_local<<<hb, 32 * HP_WARPS, 0, s>>>(r->bc, n, r->dyn_local, r->dyn_csum, z == 5 ? 1 : 0, r->ss);
         }
         {
             ProfScope ps(c, KP_SAMPLER, 0);
-            k_hprefix_csum<<<1, 32, 0, s>>>(r->dyn_csum, nbB, r->ss);
+            k_hprefix_csum<<<1, 1024, 0, s>>>(r->dyn_csum, nbB, r->ss);
         }
     }
     if (dyn_d) {
@@ -710,11 +816,11 @@ int sr_draw(axbc_ctx *c, SampledRun *r)
         D.d_csum = r->dyn_csum2;
         {
             ProfScope ps(c, KP_SAMPLER, (double)n * 12.0);
-            k_hprefix_local<<<hb, 128, 0, s>>>(r->delta_last, n, r->dyn_local2, r->dyn_csum2, 0, r->ss);
+            k_hprefix_local<<<hb, 32 * HP_WARPS, 0, s>>>(r->delta_last, n, r->dyn_local2, r->dyn_csum2, 0, r->ss);
         }
         {
             ProfScope ps(c, KP_SAMPLER, 0);
-            k_hprefix_csum<<<1, 32, 0, s>>>(r->dyn_csum2, nbB, r->ss);
+            k_hprefix_csum<<<1, 1024, 0, s>>>(r->dyn_csum2, nbB, r->ss);
         }
     }
     {
@@ -889,7 +995,7 @@ __global__ void k_sample_one(SamplerDists D, int z, uint64_t N, int first, doubl
     }
     uint32_t v0 = 0;
     double prob = 0;
-    d_draw_one(x, mix, z, N, D, first != 0, S_bc, S_d, S_lcc, v0, prob);
+    d_draw_one<false>(x, mix, z, N, D, first != 0, S_bc, S_d, S_lcc, v0, prob);
     state[0] = x;
     state[1] = mix;
     *out_v = v0;
@@ -928,18 +1034,18 @@ extern "C" int axbc_sample(axbc_ctx *c, int z, uint64_t *rng, uint32_t *mix, int
     D.bc = c->bc;
     D.delta_last = c->delta_last;
     const uint64_t nbB = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
-    const unsigned hb = (unsigned)((nbB + 127) / 128);
+    const unsigned hb = (unsigned)min((uint64_t)65535, (nbB + HP_WARPS - 1) / HP_WARPS);
     if (!first && (z == 3 || z == 5 || z == 6)) {
         D.bc_local = c->dyn_local;
         D.bc_csum = c->dyn_csum;
-        k_hprefix_local<<<hb, 128, 0, s>>>(c->bc, n, c->dyn_local, c->dyn_csum, z == 5 ? 1 : 0, nullptr);
-        k_hprefix_csum<<<1, 32, 0, s>>>(c->dyn_csum, nbB, nullptr);
+        k_hprefix_local<<<hb, 32 * HP_WARPS, 0, s>>>(c->bc, n, c->dyn_local, c->dyn_csum, z == 5 ? 1 : 0, nullptr);
+        k_hprefix_csum<<<1, 1024, 0, s>>>(c->dyn_csum, nbB, nullptr);
     }
     if (!first && (z == 4 || z == 6)) {
         D.d_local = c->dyn_local2;
         D.d_csum = c->dyn_csum2;
-        k_hprefix_local<<<hb, 128, 0, s>>>(c->delta_last, n, c->dyn_local2, c->dyn_csum2, 0, nullptr);
-        k_hprefix_csum<<<1, 32, 0, s>>>(c->dyn_csum2, nbB, nullptr);
+        k_hprefix_local<<<hb, 32 * HP_WARPS, 0, s>>>(c->delta_last, n, c->dyn_local2, c->dyn_csum2, 0, nullptr);
+        k_hprefix_csum<<<1, 1024, 0, s>>>(c->dyn_csum2, nbB, nullptr);
     }
     // state, v0, p through the check-value scratch of the context
     uint64_t *dstate = nullptr;

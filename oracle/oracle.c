@@ -525,23 +525,39 @@ void orc_lcc(const orc_graph *g, float *out)
 /* Hierarchical prefix used for every float-weighted distribution (the
  * reference's prefix_by_row_float / prefix_by_col_float, src/axbc2d.c:
  * 1985-2058 and 2105-2139, accumulate in float left to right; here the sums
- * are double, block-local running sums plus a running sum of block totals, so
- * the device computes identical values in parallel). */
+ * are double and two-level at both the element and the block scale, so that
+ * no chain of dependent additions is longer than about 32 + n/32768 and the
+ * device computes identical values in parallel). */
 void orc_hprefix(const float *w, uint64_t n, double *local, double *csum)
 {
-    const uint64_t B = ORC_SAMPLE_BLOCK;
+    /* Two-level running sums in double, each level left to right:
+     *  - a block of 1024 weights is 32 runs of 32; s = running sum inside the
+     *    run, P = running sum of the finished runs' totals; local[i] = P + s;
+     *    the block total is P after its last run;
+     *  - blocks form groups of 32: L = running sum of block totals inside the
+     *    group, G = running sum of the finished groups' totals; csum[b] = G + L.
+     * The prefix is monotone for non-negative weights; the search below is
+     * block-first, then inside the block. */
+    const uint64_t B = ORC_SAMPLE_BLOCK, R = 32;
     const uint64_t nb = (n + B - 1) / B;
-    uint64_t b, i;
-    double c = 0.0;
+    uint64_t b, j, i;
+    double G = 0.0, L = 0.0;
     for (b = 0; b < nb; b++) {
-        double t = 0.0;
-        uint64_t e = (b + 1) * B < n ? (b + 1) * B : n;
-        for (i = b * B; i < e; i++) {
-            t = t + (double)w[i];
-            local[i] = t;
+        double P = 0.0;
+        const uint64_t e = (b + 1) * B < n ? (b + 1) * B : n;
+        for (j = b * B; j < e; j += R) {
+            const uint64_t je = j + R < e ? j + R : e;
+            double s = 0.0;
+            for (i = j; i < je; i++) {
+                s = s + (double)w[i];
+                local[i] = P + s;
+            }
+            P = P + s;
         }
-        c = c + t;
-        csum[b] = c;
+        if (b % R == 0) L = 0.0;
+        L = L + P;
+        csum[b] = G + L;
+        if (b % R == R - 1 || b == nb - 1) G = G + L;
     }
 }
 

@@ -102,7 +102,8 @@ int orc_bc_pivots_omp(const orc_graph *g, const uint32_t *v0, const double *p, u
 void orc_degree2(const orc_graph *g, uint32_t *out);          /* (uint32)(deg*deg) */
 void orc_sum_deg_neigh(const orc_graph *g, uint32_t *out);    /* sum of neighbour degrees */
 void orc_lcc(const orc_graph *g, float *out);                  /* lcc_func */
-/* hierarchical prefix: local[n] block-local running sums, csum[nb] block sums' running sums */
+/* hierarchical prefix: local[n] in-block prefix (runs of 32 inside blocks of
+ * 1024), csum[nb] prefix of block totals (groups of 32 blocks) */
 void orc_hprefix(const float *w, uint64_t n, double *local, double *csum);
 uint64_t orc_hsearch(const double *local, const double *csum, uint64_t n, double r, int *found);
 

@@ -280,3 +280,50 @@ def test_restated_generator_stages(orc):
     assert np.array_equal(np.minimum(a, b), s1[ok, 0]) and np.array_equal(np.maximum(a, b), s1[ok, 1])
     mapped = img[img >= 0]
     assert len(np.unique(mapped)) == len(mapped)
+
+
+def _hprefix_py(w):
+    """The two-level prefix in plain Python floats (IEEE double, left to right
+    at every level): runs of 32 inside blocks of 1024, groups of 32 blocks."""
+    n = len(w)
+    nb = (n + 1023) // 1024
+    local = [0.0] * n
+    csum = [0.0] * nb
+    G = L = 0.0
+    for b in range(nb):
+        P = 0.0
+        for j in range(b * 1024, min(n, (b + 1) * 1024), 32):
+            s = 0.0
+            for i in range(j, min(j + 32, (b + 1) * 1024, n)):
+                s = s + float(w[i])
+                local[i] = P + s
+            P = P + s
+        if b % 32 == 0:
+            L = 0.0
+        L = L + P
+        csum[b] = G + L
+        if b % 32 == 31 or b == nb - 1:
+            G = G + L
+    return np.array(local), np.array(csum)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 1024, 1025, 5000, 33 * 1024 + 77])
+def test_hprefix_definition(orc, n):
+    rng = np.random.default_rng(n)
+    w = (rng.random(n) * rng.choice([1e-3, 1.0, 1e6], n)).astype(np.float32)
+    w[rng.random(n) < 0.2] = 0.0
+    local, csum = orc.hprefix(w)
+    wl, wc = _hprefix_py(w)
+    assert np.array_equal(local, wl) and np.array_equal(csum, wc)
+    assert (np.diff(csum) >= 0).all()
+    for b in range(len(csum)):
+        blk = local[b * 1024:(b + 1) * 1024]
+        assert (np.diff(blk) >= 0).all()
+    np.testing.assert_allclose(csum[-1], np.sum(w, dtype=np.float64), rtol=1e-12)
+    # the search returns the first index whose (exact) prefix reaches r
+    for r in rng.random(50) * csum[-1]:
+        i, found = orc.hsearch(local, csum, float(r))
+        assert found
+        b = i // 1024
+        full = (csum[b - 1] if b else 0.0) + local[i]
+        assert full >= r * (1 - 1e-12)
