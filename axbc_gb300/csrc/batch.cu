@@ -735,9 +735,10 @@ __device__ __forceinline__ float tree8(const uint4 *su4, const uint4 *sg4, int g
 // the reference's ((delta + 1) / sigma[r]) * sigma[c].  The 32 positions of a
 // chunk form four 8-position subtrees of the canonical tree; a subtree without
 // successors sums to +0 and is skipped.
-__device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, uint32_t b0,
-                                          uint32_t b1, const uint32_t *__restrict__ fnext,
-                                          const float *__restrict__ mq, uint32_t *su, uint32_t *sg)
+// `un` holds the adjacency entries of the first chunk (row[b0 + lane]).
+__device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float sv, uint32_t b0,
+                                               uint32_t b1, uint32_t un, const uint32_t *__restrict__ fnext,
+                                               const float *__restrict__ mq, uint32_t *su, uint32_t *sg)
 {
     const unsigned lane = lane_id();
     const uint32_t lanebit = 1u << lane;
@@ -746,7 +747,6 @@ __device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, ui
     const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
     float P = 0.0f;
     // the next chunk's adjacency entries load while this chunk is consumed
-    uint32_t un = b0 + lane < b1 ? a.row[b0 + lane] : 0u;
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
         const uint32_t u = un;
@@ -766,6 +766,14 @@ __device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, ui
         __syncwarp();
     }
     return P;
+}
+
+__device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, uint32_t b0,
+                                          uint32_t b1, const uint32_t *__restrict__ fnext,
+                                          const float *__restrict__ mq, uint32_t *su, uint32_t *sg)
+{
+    const uint32_t e = b0 + lane_id();
+    return dep_span_from(a, f, sv, b0, b1, e < b1 ? a.row[e] : 0u, fnext, mq, su, sg);
 }
 
 // delta and q of vertex v for the pivots in f
@@ -789,16 +797,34 @@ __device__ __forceinline__ void bwd_vertices(const Adj &a, uint32_t v_l, uint32_
 {
     const unsigned lane = lane_id();
     unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
-    while (act) {
-        const int j = __ffs(act) - 1;
+    if (!act) return;
+    // the adjacency bounds of all listed vertices load at once; the first
+    // chunk of the next vertex's adjacency loads while a vertex is summed
+    uint32_t c0_l = 0, c1_l = 0;
+    if (f_l && !no_succ) {
+        c0_l = a.col[v_l];
+        c1_l = a.col[v_l + 1];
+    }
+    int j = __ffs(act) - 1;
+    uint32_t b0 = __shfl_sync(FULL_MASK, c0_l, j), b1 = __shfl_sync(FULL_MASK, c1_l, j);
+    uint32_t un = b0 + lane < b1 ? a.row[b0 + lane] : 0u;
+    for (;;) {
         act &= act - 1;
         const uint32_t v = __shfl_sync(FULL_MASK, v_l, j);
         const uint32_t f = __shfl_sync(FULL_MASK, f_l, j);
+        const uint32_t cb0 = b0, cb1 = b1, cu = un;
+        const int jn = act ? __ffs(act) - 1 : -1;
+        if (jn >= 0) {
+            b0 = __shfl_sync(FULL_MASK, c0_l, jn);
+            b1 = __shfl_sync(FULL_MASK, c1_l, jn);
+            un = b0 + lane < b1 ? a.row[b0 + lane] : 0u;
+        }
         const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
         float P = 0.0f;
-        if (!no_succ)
-            P = dep_span(a, f, __uint2float_rn(sig), a.col[v], a.col[v + 1], fnext, mq, su, sg);
+        if (!no_succ) P = dep_span_from(a, f, __uint2float_rn(sig), cb0, cb1, cu, fnext, mq, su, sg);
         write_dep(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
+        if (jn < 0) break;
+        j = jn;
     }
 }
 
