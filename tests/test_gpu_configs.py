@@ -1,6 +1,7 @@
 """The benchmark configurations as parity cases at full size.
 
-Config 2: Kronecker scale 20, one-degree reduction (-H 1), heuristic 1, width 64.
+Config 1: the reference's scale-14 graph, -z 0 -N 256, seed 1.
+Config 2: the reference's scale-20 graph, one-degree reduction (-H 1), heuristic 1, width 64.
 Config 3: 2048x2048 grid, 2% of edges dropped (seed 7), 0.01% long-range edges,
 heuristic 4 with Bader's stop (-c 1 -x 8).  On this graph uint32 path counts
 wrap and floats overflow (hundreds of BFS levels): comparisons are type for
@@ -90,3 +91,23 @@ def test_config3_grid_sampled_adaptive_matches_oracle(axbc, orc, grid2048):
     assert np.array_equal(got["pivots"], want["pivots"])
     assert got["nrounds"] == want["nrounds"] and got["stopped"] == want["stopped"]
     same_floats(ctx.bc(), want["bc"], "grid sampled bc")
+
+
+@pytest.mark.parametrize("W", [1, 32])
+def test_config1_scale14_z0_sampled(axbc, orc, W):
+    """Config 1: the reference's scale-14 graph (Graph500 generator, seeds
+    23/24, built on the device), -H 0 -z 0 -N 256 -c 0, seed 1: the whole run
+    bit for bit against the oracle on the reference pipeline's CSC of the
+    restated generator's edges."""
+    G = axbc.Graph.kronecker(14, 16)
+    g = orc.pipeline(orc.kron_edges(14, 16).astype(np.uint64), 1 << 14, True, 0)
+    col, row, _ = G.csc()
+    assert np.array_equal(col, g.col) and np.array_equal(row, g.row)
+    assert g.m == 430200
+    ctx = axbc.Context(G)
+    got = ctx.run_sampled(z=0, nbfs=256, bader_c=0, nchecks=1, H=0, seed=1, W=W)
+    want = orc.run(g, z=0, nbfs=256, bader_c=0, nchecks=1, H=0, seed=1, W=W)
+    assert np.array_equal(got["pivots"], want["pivots"])
+    for k in ("nrounds", "skipped", "dropped", "te"):
+        assert got[k] == want[k], k
+    same_floats(ctx.bc(), want["bc"], "bc, config 1")
