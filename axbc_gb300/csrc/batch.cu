@@ -1400,7 +1400,11 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     const size_t ctl_off = offsetof(BatchInfo, cur);
     const size_t ctl_len = offsetof(BatchInfo, push_factor) - ctl_off;
     const size_t prof_first = c->prof.size();
-    int launched = 0, K = 8;
+    // forward steps launched before the first look at `alive`: one more than
+    // the last batch needed, so a batch like it ends after one host round
+    // trip; later groups double
+    int launched = 0, K = std::max(4, std::min(256, c->last_batch_levels + 1));
+    if (c->last_batch_levels == 0) K = 8;
     for (;;) {
         TRY(axbc_batch_levels_alloc(c, launched + K + 2));
         for (int i = 0; i < K; i++) {
@@ -1454,9 +1458,12 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         lte.resize(L + 1);
         lcnt.resize(L + 1);
         lmode.resize(L + 1);
-        CU(cudaMemcpy(lte.data(), c->d_level_te, (L + 1) * 8, cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(lcnt.data(), c->d_level_cnt, (L + 1) * 8, cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(lmode.data(), c->d_level_mode, (L + 1) * 4, cudaMemcpyDeviceToHost));
+        // one wait for the three per-level arrays and the depth-0 mask
+        CU(cudaMemcpyAsync(lte.data(), c->d_level_te, (L + 1) * 8, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(lcnt.data(), c->d_level_cnt, (L + 1) * 8, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(lmode.data(), c->d_level_mode, (L + 1) * 4, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(&c->bi_host->depth0mask, &c->bi->depth0mask, 4, cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
         const double W = nsrc;
         for (size_t i = prof_first; i < c->prof.size(); i++) {
             ProfRec &r = c->prof[i];
@@ -1480,9 +1487,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
                 c->launches += g->fwd.n_heavy ? 3 : 2;
                 continue;
             }
-            if (d == Dmax) {
-                CU(cudaMemcpy(&depth0, &c->bi->depth0mask, 4, cudaMemcpyDeviceToHost));
-            }
+            if (d == Dmax) depth0 = c->bi_host->depth0mask;
             const double W = nsrc;
             double te_d = (double)lte[d], cnt_d = (double)lcnt[d];
             if (d == 0) {
