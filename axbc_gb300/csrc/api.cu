@@ -226,6 +226,7 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     axbc_dfree(c->wtmp);
     prof_clear(c);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    if (c->rb_ev) cudaEventDestroy(c->rb_ev);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return AXBC_OK;

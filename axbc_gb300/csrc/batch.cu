@@ -1364,6 +1364,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         c->launches++;
     }
     c->prev_lend = 0;
+    TRY(axbc_batch_settle(c));
     if (c->pool_short && c->lpool_cap < 32 * n + 64) {
         CU(cudaStreamSynchronize(s));
         axbc_dfree(c->lpool);
@@ -1513,14 +1514,26 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         }
         CU_LAUNCH("backward levels");
     }
+    // the per-pivot level counts and the list-pool flag arrive in the
+    // background; the next batch (or a caller that reports them) waits for them
+    if (!c->rb_ev) CU(cudaEventCreateWithFlags(&c->rb_ev, cudaEventDisableTiming));
     CU(cudaMemcpyAsync(c->bi_host->Ls, c->bi->Ls, sizeof(c->bi_host->Ls), cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(&c->bi_host->pool_short, &c->bi->pool_short, 4, cudaMemcpyDeviceToHost, s));
-    CU(cudaStreamSynchronize(s));
+    CU(cudaEventRecord(c->rb_ev, s));
+    c->rb_pending = true;
     c->last_batch_levels = L;
     c->last_batch_nsrc = nsrc;
     c->prev_lend = L;
+    return AXBC_OK;
+}
+
+int axbc_batch_settle(axbc_ctx *c)
+{
+    if (!c->rb_pending) return AXBC_OK;
+    CU(cudaEventSynchronize(c->rb_ev));
+    c->rb_pending = false;
     c->pool_short = c->bi_host->pool_short != 0;
-    for (int i = 0; i < AXBC_W; i++) c->last_Ls[i] = i < nsrc ? c->bi_host->Ls[i] : 0;
+    for (int i = 0; i < AXBC_W; i++) c->last_Ls[i] = i < c->last_batch_nsrc ? c->bi_host->Ls[i] : 0;
     return AXBC_OK;
 }
 
@@ -1611,6 +1624,7 @@ extern "C" int axbc_run_batch(axbc_ctx *c, const uint32_t *v0, const double *p, 
     CU(cudaMemcpyAsync(&c->bi->p, c->bi_host->p, sizeof(c->bi_host->p), cudaMemcpyHostToDevice, s));
     TRY(axbc_batch_traverse(c, k, H));
     TRY(axbc_batch_apply(c));
+    TRY(axbc_batch_settle(c));
     if (stats) {
         CU(cudaMemcpyAsync(c->bi_host, c->bi, sizeof(BatchInfo), cudaMemcpyDeviceToHost, s));
         std::vector<uint32_t> rr(k);

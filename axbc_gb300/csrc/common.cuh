@@ -227,6 +227,10 @@ struct axbc_ctx {
     int last_batch_levels = 0;
     int last_batch_nsrc = 0;
     int last_Ls[AXBC_W] = {0};  // first empty level of each pivot of the last batch
+    // the last batch's per-pivot level counts and list-pool flag are read back
+    // without waiting; rb_ev marks their arrival (axbc_batch_settle)
+    cudaEvent_t rb_ev = nullptr;
+    bool rb_pending = false;
     // sampler
     SamplerState *ss = nullptr;
     SamplerState *ss_host = nullptr;  // pinned
@@ -283,6 +287,7 @@ int axbc_single_update(axbc_ctx *c, uint32_t v0, double p, const uint32_t *reach
                        uint64_t nvt_base, int add_all, int add_sum);
 int axbc_ensure_batch(axbc_ctx *c);
 int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H);
+int axbc_batch_settle(axbc_ctx *c);
 int axbc_batch_apply(axbc_ctx *c);
 int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo,
                            const int *lane_hi, int nseg);
