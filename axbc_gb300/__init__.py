@@ -124,6 +124,8 @@ _SIGS = {
     "axbc_ctx_profile_records": (C.c_int, [_P, _P, _P, _P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "axbc_srand48": (C.c_uint64, [C.c_int64]),
     "axbc_inject_alloc_failures": (None, [C.c_int]),
+    "axbc_inject_alloc_failure_after": (None, [C.c_int]),
+    "axbc_device_bytes_live": (C.c_uint64, []),
     "axbc_sample": (C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int,
                               C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "axbc_bader_check": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(C.c_int)]),

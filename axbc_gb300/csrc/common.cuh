@@ -276,6 +276,22 @@ int axbc_kron_device(int scale, int edgefactor, uint64_t seed1, uint64_t seed2, 
 int axbc_dalloc(void **p, size_t bytes, uint64_t *acct);
 void axbc_dfree(void *p);
 
+// a scratch device buffer freed when it goes out of scope (error paths included)
+struct DBuf {
+    void *p = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { axbc_dfree(p); }
+    int alloc(size_t bytes) { return axbc_dalloc(&p, bytes, nullptr); }
+    void release()
+    {
+        axbc_dfree(p);
+        p = nullptr;
+    }
+    template <class T> T *as() const { return (T *)p; }
+};
+
 // single.cu / batch.cu
 int axbc_ensure_single(axbc_ctx *c);
 int axbc_single_reset(axbc_ctx *c);

@@ -8,29 +8,59 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
 
-// failure injection for tests: the next n device allocations fail
+// failure injection for tests: the next n device allocations fail; or, armed
+// with a skip count, the allocation after the next `skip` fails
 static std::atomic<int> g_fail_allocs{0};
+static std::atomic<int> g_fail_after{-1};
 
 extern "C" void axbc_inject_alloc_failures(int n) { g_fail_allocs.store(n < 0 ? 0 : n); }
+extern "C" void axbc_inject_alloc_failure_after(int skip) { g_fail_after.store(skip < 0 ? -1 : skip); }
+
+// device bytes the library holds, for leak checks
+static std::mutex g_live_mu;
+static std::unordered_map<void *, size_t> g_live;
+static uint64_t g_live_bytes = 0;
+
+extern "C" uint64_t axbc_device_bytes_live(void)
+{
+    std::lock_guard<std::mutex> lk(g_live_mu);
+    return g_live_bytes;
+}
+
+static bool injected_failure()
+{
+    for (int k = g_fail_allocs.load(); k > 0; k = g_fail_allocs.load())
+        if (g_fail_allocs.compare_exchange_weak(k, k - 1)) return true;
+    for (int k = g_fail_after.load(); k >= 0; k = g_fail_after.load())
+        if (g_fail_after.compare_exchange_weak(k, k - 1)) return k == 0;
+    return false;
+}
 
 int axbc_dalloc(void **p, size_t bytes, uint64_t *acct)
 {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
-    for (int k = g_fail_allocs.load(); k > 0; k = g_fail_allocs.load())
-        if (g_fail_allocs.compare_exchange_weak(k, k - 1)) {
-            axbc_set_error("device allocation of %zu bytes refused (injected failure)", bytes);
-            return AXBC_ERR_NOMEM;
-        }
+    if (injected_failure()) {
+        axbc_set_error("device allocation of %zu bytes refused (injected failure)", bytes);
+        return AXBC_ERR_NOMEM;
+    }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
+        *p = nullptr;
         axbc_set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
         return AXBC_ERR_NOMEM;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_live_mu);
+        g_live[*p] = bytes;
+        g_live_bytes += bytes;
     }
     if (acct) *acct += bytes;
     return AXBC_OK;
@@ -38,7 +68,16 @@ int axbc_dalloc(void **p, size_t bytes, uint64_t *acct)
 
 void axbc_dfree(void *p)
 {
-    if (p) cudaFree(p);
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lk(g_live_mu);
+        auto it = g_live.find(p);
+        if (it != g_live.end()) {
+            g_live_bytes -= it->second;
+            g_live.erase(it);
+        }
+    }
+    cudaFree(p);
 }
 
 // ------------------------------------------------------------------ upload
@@ -479,52 +518,43 @@ __global__ void k_leaf_reduce(const uint64_t *__restrict__ keys, uint64_t m, con
 // and wrap it in a graph.
 
 int axbc_keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetric, int H,
-                         axbc_graph **out)
+                       axbc_graph **out)
 {
     cudaStream_t s = 0;
-    uint64_t *d_sorted = nullptr;
-    void *d_tmp = nullptr;
     size_t tmp_bytes = 0;
-    int rc = AXBC_OK;
-    TRY(axbc_dalloc((void **)&d_sorted, nk * 8, nullptr));
-    // all 64 bits: the all-ones padding keys must sort last
-    cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, d_keys, d_sorted, (int64_t)nk, 0, 64, s);
-    rc = axbc_dalloc(&d_tmp, tmp_bytes, nullptr);
-    if (rc) {
-        axbc_dfree(d_sorted);
-        return rc;
-    }
-    cub::DeviceRadixSort::SortKeys(d_tmp, tmp_bytes, d_keys, d_sorted, (int64_t)nk, 0, 64, s);
-    axbc_dfree(d_tmp);
-    CU_LAUNCH("radix sort");
-
-    unsigned long long *d_min = nullptr;
-    TRY(axbc_dalloc((void **)&d_min, 8, nullptr));
-    CU(cudaMemset(d_min, 0xff, 8));
-    k_min_uv<<<1024, 256>>>(d_sorted, nk, d_min);
-    unsigned long long minuv = ~0ull;
-    CU(cudaMemcpy(&minuv, d_min, 8, cudaMemcpyDeviceToHost));
-    axbc_dfree(d_min);
-    uint64_t quirk = ~0ull;
-    if (minuv != ~0ull && (uint32_t)(minuv >> 32) == (uint32_t)minuv) quirk = ckey((uint32_t)minuv, (uint32_t)minuv);
-
-    uint8_t *d_flag = nullptr;
-    TRY(axbc_dalloc((void **)&d_flag, nk, nullptr));
-    k_mark<<<2048, 256>>>(d_sorted, nk, quirk, d_flag);
-    CU_LAUNCH("k_mark");
-    unsigned long long *d_nsel = nullptr;
-    TRY(axbc_dalloc((void **)&d_nsel, 8, nullptr));
-    tmp_bytes = 0;
-    cub::DeviceSelect::Flagged(nullptr, tmp_bytes, d_sorted, d_flag, d_keys, d_nsel, (int64_t)nk, s);
-    TRY(axbc_dalloc(&d_tmp, tmp_bytes, nullptr));
-    cub::DeviceSelect::Flagged(d_tmp, tmp_bytes, d_sorted, d_flag, d_keys, d_nsel, (int64_t)nk, s);
-    CU_LAUNCH("select");
     unsigned long long m = 0;
-    CU(cudaMemcpy(&m, d_nsel, 8, cudaMemcpyDeviceToHost));
-    axbc_dfree(d_tmp);
-    axbc_dfree(d_nsel);
-    axbc_dfree(d_flag);
-    axbc_dfree(d_sorted);
+    {
+        DBuf sorted, tmp, mn, flag, nsel;
+        TRY(sorted.alloc(nk * 8));
+        // all 64 bits: the all-ones padding keys must sort last
+        cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, d_keys, sorted.as<uint64_t>(), (int64_t)nk, 0, 64, s);
+        TRY(tmp.alloc(tmp_bytes));
+        cub::DeviceRadixSort::SortKeys(tmp.p, tmp_bytes, d_keys, sorted.as<uint64_t>(), (int64_t)nk, 0, 64, s);
+        CU_LAUNCH("radix sort");
+        tmp.release();
+
+        TRY(mn.alloc(8));
+        CU(cudaMemset(mn.p, 0xff, 8));
+        k_min_uv<<<1024, 256>>>(sorted.as<uint64_t>(), nk, mn.as<unsigned long long>());
+        unsigned long long minuv = ~0ull;
+        CU(cudaMemcpy(&minuv, mn.p, 8, cudaMemcpyDeviceToHost));
+        uint64_t quirk = ~0ull;
+        if (minuv != ~0ull && (uint32_t)(minuv >> 32) == (uint32_t)minuv)
+            quirk = ckey((uint32_t)minuv, (uint32_t)minuv);
+
+        TRY(flag.alloc(nk));
+        k_mark<<<2048, 256>>>(sorted.as<uint64_t>(), nk, quirk, flag.as<uint8_t>());
+        CU_LAUNCH("k_mark");
+        TRY(nsel.alloc(8));
+        tmp_bytes = 0;
+        cub::DeviceSelect::Flagged(nullptr, tmp_bytes, sorted.as<uint64_t>(), flag.as<uint8_t>(), d_keys,
+                                   nsel.as<unsigned long long>(), (int64_t)nk, s);
+        TRY(tmp.alloc(tmp_bytes));
+        cub::DeviceSelect::Flagged(tmp.p, tmp_bytes, sorted.as<uint64_t>(), flag.as<uint8_t>(), d_keys,
+                                   nsel.as<unsigned long long>(), (int64_t)nk, s);
+        CU_LAUNCH("select");
+        CU(cudaMemcpy(&m, nsel.p, 8, cudaMemcpyDeviceToHost));
+    }
     if (m >= 0xffffffffull) {
         axbc_set_error("graph has %llu adjacency entries; 32-bit offsets hold < 2^32", m);
         return AXBC_ERR_RANGE;
@@ -536,55 +566,48 @@ int axbc_keys_to_graph(uint64_t *d_keys, uint64_t nk, uint64_t n, int symmetric,
             axbc_set_error("one-degree reduction of a generated graph needs a symmetric graph");
             return AXBC_ERR_INVALID;
         }
-        uint8_t *d_leafv = nullptr, *d_kind = nullptr;
-        uint32_t *d_reach = nullptr;
-        unsigned long long *d_last = nullptr;
-        TRY(axbc_dalloc((void **)&d_leafv, n, nullptr));
-        TRY(axbc_dalloc((void **)&d_kind, m, nullptr));
-        TRY(axbc_dalloc((void **)&d_reach, n * 4, nullptr));
-        TRY(axbc_dalloc((void **)&d_last, 8, nullptr));
-        CU(cudaMemset(d_leafv, 0, n));
-        CU(cudaMemset(d_reach, 0, n * 4));
-        CU(cudaMemset(d_last, 0, 8));
-        k_leaf_entries<<<2048, 256>>>(d_keys, m, d_leafv, d_kind, d_last);
+        DBuf leafv, kind, dreach, last, kept, nsel, tmp;
+        TRY(leafv.alloc(n));
+        TRY(kind.alloc(m));
+        TRY(dreach.alloc(n * 4));
+        TRY(last.alloc(8));
+        CU(cudaMemset(leafv.p, 0, n));
+        CU(cudaMemset(dreach.p, 0, n * 4));
+        CU(cudaMemset(last.p, 0, 8));
+        k_leaf_entries<<<2048, 256>>>(d_keys, m, leafv.as<uint8_t>(), kind.as<uint8_t>(),
+                                      last.as<unsigned long long>());
         CU_LAUNCH("k_leaf_entries");
-        k_leaf_reduce<<<2048, 256>>>(d_keys, m, d_leafv, d_kind, d_reach, d_last);
+        k_leaf_reduce<<<2048, 256>>>(d_keys, m, leafv.as<uint8_t>(), kind.as<uint8_t>(), dreach.as<uint32_t>(),
+                                     last.as<unsigned long long>());
         CU_LAUNCH("k_leaf_reduce");
-        uint64_t *d_kept = nullptr;
-        TRY(axbc_dalloc((void **)&d_kept, m * 8, nullptr));
-        TRY(axbc_dalloc((void **)&d_nsel, 8, nullptr));
+        TRY(kept.alloc(m * 8));
+        TRY(nsel.alloc(8));
         tmp_bytes = 0;
-        cub::DeviceSelect::Flagged(nullptr, tmp_bytes, d_keys, d_kind, d_kept, d_nsel, (int64_t)m, s);
-        TRY(axbc_dalloc(&d_tmp, tmp_bytes, nullptr));
-        cub::DeviceSelect::Flagged(d_tmp, tmp_bytes, d_keys, d_kind, d_kept, d_nsel, (int64_t)m, s);
+        cub::DeviceSelect::Flagged(nullptr, tmp_bytes, d_keys, kind.as<uint8_t>(), kept.as<uint64_t>(),
+                                   nsel.as<unsigned long long>(), (int64_t)m, s);
+        TRY(tmp.alloc(tmp_bytes));
+        cub::DeviceSelect::Flagged(tmp.p, tmp_bytes, d_keys, kind.as<uint8_t>(), kept.as<uint64_t>(),
+                                   nsel.as<unsigned long long>(), (int64_t)m, s);
         CU_LAUNCH("select kept entries");
-        CU(cudaMemcpy(&m, d_nsel, 8, cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(d_keys, d_kept, m * 8, cudaMemcpyDeviceToDevice));
+        CU(cudaMemcpy(&m, nsel.p, 8, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(d_keys, kept.p, m * 8, cudaMemcpyDeviceToDevice));
         reach.resize(n);
-        CU(cudaMemcpy(reach.data(), d_reach, n * 4, cudaMemcpyDeviceToHost));
-        axbc_dfree(d_tmp);
-        axbc_dfree(d_nsel);
-        axbc_dfree(d_kept);
-        axbc_dfree(d_last);
-        axbc_dfree(d_reach);
-        axbc_dfree(d_kind);
-        axbc_dfree(d_leafv);
+        CU(cudaMemcpy(reach.data(), dreach.p, n * 4, cudaMemcpyDeviceToHost));
     }
 
-    uint32_t *d_row = nullptr, *d_cnt = nullptr;
-    TRY(axbc_dalloc((void **)&d_row, m * 4, nullptr));
-    TRY(axbc_dalloc((void **)&d_cnt, (n + 1) * 4, nullptr));
-    CU(cudaMemset(d_cnt, 0, (n + 1) * 4));
-    k_split<<<2048, 256>>>(d_keys, m, d_row, d_cnt);
-    CU_LAUNCH("k_split");
-    std::vector<uint32_t> col(n + 1), cnt(n + 1);
-    CU(cudaMemcpy(cnt.data(), d_cnt, (n + 1) * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> col(n + 1), cnt(n + 1), row(m);
+    {
+        DBuf drow, dcnt;
+        TRY(drow.alloc(m * 4));
+        TRY(dcnt.alloc((n + 1) * 4));
+        CU(cudaMemset(dcnt.p, 0, (n + 1) * 4));
+        k_split<<<2048, 256>>>(d_keys, m, drow.as<uint32_t>(), dcnt.as<uint32_t>());
+        CU_LAUNCH("k_split");
+        CU(cudaMemcpy(cnt.data(), dcnt.p, (n + 1) * 4, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(row.data(), drow.p, m * 4, cudaMemcpyDeviceToHost));
+    }
     col[0] = 0;
     for (uint64_t v = 0; v < n; v++) col[v + 1] = col[v] + cnt[v];
-    std::vector<uint32_t> row(m);
-    CU(cudaMemcpy(row.data(), d_row, m * 4, cudaMemcpyDeviceToHost));
-    axbc_dfree(d_row);
-    axbc_dfree(d_cnt);
     return graph_from_host(col.data(), row.data(), n, m, reach.empty() ? nullptr : reach.data(), symmetric, out);
 }
 
@@ -620,33 +643,24 @@ extern "C" int axbc_graph_from_edges(const uint64_t *edges, uint64_t nedges, uin
               "axbc_graph_from_edges: the one-degree reduction runs on undirected graphs here "
               "(axbc_edges_to_csc takes directed ones)");
     const uint64_t nk = undirected ? 2 * nedges : nedges;
-    uint64_t *d_edges = nullptr, *d_keys = nullptr;
-    int *d_bad = nullptr;
-    int rc = AXBC_OK;
     if (nk == 0) return graph_from_host(std::vector<uint32_t>(n + 1, 0).data(), nullptr, n, 0, nullptr, 1, g);
-    TRY(axbc_dalloc((void **)&d_bad, sizeof(int), nullptr));
-    rc = axbc_dalloc((void **)&d_edges, nedges * 16, nullptr);
-    if (!rc) rc = axbc_dalloc((void **)&d_keys, nk * 8, nullptr);
-    if (!rc) {
-        int bad = 0;
-        if (cudaMemset(d_bad, 0, sizeof(int)) != cudaSuccess ||
-            cudaMemcpy(d_edges, edges, nedges * 16, cudaMemcpyHostToDevice) != cudaSuccess) {
-            rc = axbc_cuda_fail(cudaGetLastError(), "edge upload", __FILE__, __LINE__);
-        } else {
-            k_list_to_keys<<<2048, 256>>>(d_edges, nedges, n, undirected, d_keys, d_bad);
-            if (cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-                rc = axbc_cuda_fail(cudaGetLastError(), "k_list_to_keys", __FILE__, __LINE__);
-            else if (bad) {
-                axbc_set_error("axbc_graph_from_edges: an edge has a vertex >= n");
-                rc = AXBC_ERR_INVALID;
-            }
-        }
+    DBuf bad, dedges, keys;
+    TRY(bad.alloc(sizeof(int)));
+    TRY(dedges.alloc(nedges * 16));
+    TRY(keys.alloc(nk * 8));
+    CU(cudaMemset(bad.p, 0, sizeof(int)));
+    CU(cudaMemcpy(dedges.p, edges, nedges * 16, cudaMemcpyHostToDevice));
+    k_list_to_keys<<<2048, 256>>>(dedges.as<uint64_t>(), nedges, n, undirected, keys.as<uint64_t>(),
+                                  bad.as<int>());
+    CU_LAUNCH("k_list_to_keys");
+    int hbad = 0;
+    CU(cudaMemcpy(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (hbad) {
+        axbc_set_error("axbc_graph_from_edges: an edge has a vertex >= n");
+        return AXBC_ERR_INVALID;
     }
-    axbc_dfree(d_edges);
-    axbc_dfree(d_bad);
-    if (!rc) rc = axbc_keys_to_graph(d_keys, nk, n, undirected, H, g);
-    axbc_dfree(d_keys);
-    return rc;
+    dedges.release();
+    return axbc_keys_to_graph(keys.as<uint64_t>(), nk, n, undirected, H, g);
 }
 
 extern "C" int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed, int directed,
@@ -658,13 +672,11 @@ extern "C" int axbc_graph_generate_rmat(int scale, int edgefactor, uint64_t seed
     CHECK_ARG(H == 0 || H == 1, "axbc_graph_generate_rmat: H must be 0 or 1");
     const uint64_t n = 1ull << scale;
     const uint64_t ne = n * (uint64_t)edgefactor;
-    uint64_t *d_keys = nullptr;
-    TRY(axbc_dalloc((void **)&d_keys, 2 * ne * 8, nullptr));
-    k_rmat<<<4096, 256>>>(ne, scale, seed, directed, d_keys, nullptr);
+    DBuf keys;
+    TRY(keys.alloc(2 * ne * 8));
+    k_rmat<<<4096, 256>>>(ne, scale, seed, directed, keys.as<uint64_t>(), nullptr);
     CU_LAUNCH("k_rmat");
-    int rc = axbc_keys_to_graph(d_keys, 2 * ne, n, !directed, H, g);
-    axbc_dfree(d_keys);
-    return rc;
+    return axbc_keys_to_graph(keys.as<uint64_t>(), 2 * ne, n, !directed, H, g);
 }
 
 extern "C" int axbc_graph_generate_grid(uint32_t side, double drop_prob, double longrange_frac,
@@ -675,26 +687,22 @@ extern "C" int axbc_graph_generate_grid(uint32_t side, double drop_prob, double 
     CHECK_ARG(drop_prob >= 0 && drop_prob < 1, "axbc_graph_generate_grid: bad drop probability");
     const uint64_t n = (uint64_t)side * side;
     const uint64_t nh = (uint64_t)(side - 1) * side, nv = nh, ntot = nh + nv;
-    uint64_t *d_keys = nullptr;
-    unsigned long long *d_kept = nullptr;
-    TRY(axbc_dalloc((void **)&d_kept, 8, nullptr));
-    CU(cudaMemset(d_kept, 0, 8));
+    DBuf keys, dkept;
+    TRY(dkept.alloc(8));
+    CU(cudaMemset(dkept.p, 0, 8));
     // room for the long-range edges: at most longrange_frac * ntot of them
-    uint64_t lr_cap = (uint64_t)(longrange_frac * (double)ntot) + 1;
-    TRY(axbc_dalloc((void **)&d_keys, (2 * ntot + 2 * lr_cap) * 8, nullptr));
-    uint32_t thr = (uint32_t)(drop_prob * 4294967296.0);
-    k_grid<<<2048, 256>>>(side, nh, ntot, thr, seed, d_keys, d_kept);
+    const uint64_t lr_cap = (uint64_t)(longrange_frac * (double)ntot) + 1;
+    TRY(keys.alloc((2 * ntot + 2 * lr_cap) * 8));
+    const uint32_t thr = (uint32_t)(drop_prob * 4294967296.0);
+    k_grid<<<2048, 256>>>(side, nh, ntot, thr, seed, keys.as<uint64_t>(), dkept.as<unsigned long long>());
     CU_LAUNCH("k_grid");
     unsigned long long kept = 0;
-    CU(cudaMemcpy(&kept, d_kept, 8, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(&kept, dkept.p, 8, cudaMemcpyDeviceToHost));
     uint64_t lr = (uint64_t)(longrange_frac * (double)kept);
     if (lr > lr_cap) lr = lr_cap;
-    if (lr) k_longrange<<<256, 256>>>(lr, n, seed, d_keys + 2 * ntot);
+    if (lr) k_longrange<<<256, 256>>>(lr, n, seed, keys.as<uint64_t>() + 2 * ntot);
     CU_LAUNCH("k_longrange");
-    int rc = axbc_keys_to_graph(d_keys, 2 * ntot + 2 * lr, n, 1, 0, g);
-    axbc_dfree(d_keys);
-    axbc_dfree(d_kept);
-    return rc;
+    return axbc_keys_to_graph(keys.as<uint64_t>(), 2 * ntot + 2 * lr, n, 1, 0, g);
 }
 
 // ------------------------------------------------- static distributions

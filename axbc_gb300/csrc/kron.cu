@@ -494,13 +494,6 @@ __global__ void k_edges_to_keys(const uint64_t *__restrict__ in, uint64_t m, uin
     }
 }
 
-// device buffer freed on scope exit
-struct DBuf {
-    void *p = nullptr;
-    ~DBuf() { axbc_dfree(p); }
-    template <class T> T *as() const { return (T *)p; }
-};
-
 int grid_for(uint64_t n, int tpb)
 {
     int dev = 0, sms = 152;
@@ -599,10 +592,8 @@ int axbc_kron_device(int scale, int edgefactor, uint64_t seed1, uint64_t seed2, 
         out = t;
     }
     TRY(check_err(d_err.as<int>(), "kronecker edge split"));
-    axbc_dfree(nodes_a.p);
-    nodes_a.p = nullptr;
-    axbc_dfree(nodes_b.p);
-    nodes_b.p = nullptr;
+    nodes_a.release();
+    nodes_b.release();
 
     if (stage >= 1) {
         DBuf perm;
@@ -658,7 +649,6 @@ extern "C" int axbc_graph_generate_kronecker(int scale, int edgefactor, uint64_t
     TRY(axbc_dalloc(&keys.p, 2 * m * 8, nullptr));
     k_edges_to_keys<<<grid_for(m, 256), 256>>>(e.as<uint64_t>(), m, keys.as<uint64_t>());
     CU_LAUNCH("k_edges_to_keys");
-    axbc_dfree(e.p);
-    e.p = nullptr;
+    e.release();
     return axbc_keys_to_graph(keys.as<uint64_t>(), 2 * m, 1ull << scale, 1, H, g);
 }

@@ -346,9 +346,13 @@ int axbc_ctx_profile_records(axbc_ctx *ctx, int32_t *kinds, int32_t *tags, float
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
 
-/* Test hook: the next n device allocations made by the library fail with
- * AXBC_ERR_NOMEM (host-side failure injection; 0 clears it). */
+/* Test hooks: the next n device allocations made by the library fail with
+ * AXBC_ERR_NOMEM (host-side failure injection; 0 clears it); or the
+ * allocation after the next `skip` ones fails (-1 clears it).  Device bytes the
+ * library holds at the moment, for leak checks. */
 void axbc_inject_alloc_failures(int n);
+void axbc_inject_alloc_failure_after(int skip);
+uint64_t axbc_device_bytes_live(void);
 
 /* Per forward level of the last batch (up to max_levels; *levels = all):
  * vertices newly reached over all pivots, their degree sum, direction (1:

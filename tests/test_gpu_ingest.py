@@ -73,3 +73,36 @@ def test_device_ingest_edge_cases(axbc, orc):
         axbc.Graph.from_edges(np.array([[0, 9]], np.uint64), 5)
     with pytest.raises(axbc.AxbcError):
         axbc.Graph.from_edges(np.array([[0, 1]], np.uint64), 5, undirected=False, H=1)
+
+
+def test_device_ingest_and_generator_free_everything_on_failure(axbc, orc):
+    """Every device allocation of the ingest and generator paths made to fail
+    in turn: the call reports AXBC_ERR_NOMEM, holds no device bytes afterwards,
+    and the next call succeeds."""
+    L = axbc.lib()
+    rng = np.random.default_rng(5)
+    e = rng.integers(0, 300, size=(1200, 2)).astype(np.uint64)
+    calls = [lambda: axbc.Graph.from_edges(e, 300, True, 1),
+             lambda: axbc.Graph.kronecker(8, 16, H=1),
+             lambda: axbc.Graph.rmat(8, 8, H=0),
+             lambda: axbc.Graph.grid(20, 0.02, 1e-2)]
+    for call in calls:
+        base = L.axbc_device_bytes_live()
+        failures = 0
+        for k in range(40):
+            L.axbc_inject_alloc_failure_after(k)
+            try:
+                G = call()
+            except axbc.AxbcError as ex:
+                assert ex.status == 3, ex
+                failures += 1
+                assert L.axbc_device_bytes_live() == base, f"leak after failing allocation {k}"
+                continue
+            finally:
+                L.axbc_inject_alloc_failure_after(-1)
+            G.close()
+            assert L.axbc_device_bytes_live() == base
+            break
+        else:
+            raise AssertionError("call still failing after 40 allocations")
+        assert failures >= 3
