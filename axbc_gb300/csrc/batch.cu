@@ -1196,21 +1196,25 @@ __global__ void k_source_view(int s, int levels, uint32_t *const *fm, const uint
 
 static int ensure_level_tables(axbc_ctx *c)
 {
-    if (c->fmtab) return AXBC_OK;
-    TRY(axbc_dalloc((void **)&c->fmtab, AXBC_MAX_LEVELS * sizeof(uint32_t *), &c->bytes));
-    TRY(axbc_dalloc((void **)&c->ctrs, 2 * AXBC_MAX_LEVELS * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->d_level_te, AXBC_MAX_LEVELS * 8, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->d_level_cnt, AXBC_MAX_LEVELS * 8, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->d_level_mode, AXBC_MAX_LEVELS * 4, &c->bytes));
+    if (c->tables_ready) return AXBC_OK;
+    ALLOC_MISSING(c->fmtab, AXBC_MAX_LEVELS * sizeof(uint32_t *), &c->bytes);
+    ALLOC_MISSING(c->ctrs, 2 * AXBC_MAX_LEVELS * 4, &c->bytes);
+    ALLOC_MISSING(c->d_level_te, AXBC_MAX_LEVELS * 8, &c->bytes);
+    ALLOC_MISSING(c->d_level_cnt, AXBC_MAX_LEVELS * 8, &c->bytes);
+    ALLOC_MISSING(c->d_level_mode, AXBC_MAX_LEVELS * 4, &c->bytes);
     // level lists: a vertex joins a level's list once per distinct depth at
     // which the batch's pivots reach it, so 32 n entries never run out; a
     // level may hold up to n/8 vertices before it falls back to the task scan
-    c->lpool_cap = (uint32_t)std::min<uint64_t>((uint64_t)AXBC_W * c->g->n + 64, 0xffffffffull);
-    TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)c->lpool_cap * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->lstart, AXBC_MAX_LEVELS * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->lcount, AXBC_MAX_LEVELS * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->lcap, AXBC_MAX_LEVELS * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->lheavy, AXBC_MAX_LEVELS * 4, &c->bytes));
+    if (!c->lpool) {
+        const uint32_t cap = (uint32_t)std::min<uint64_t>((uint64_t)AXBC_W * c->g->n + 64, 0xffffffffull);
+        TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)cap * 4, &c->bytes));
+        c->lpool_cap = cap;
+    }
+    ALLOC_MISSING(c->lstart, AXBC_MAX_LEVELS * 4, &c->bytes);
+    ALLOC_MISSING(c->lcount, AXBC_MAX_LEVELS * 4, &c->bytes);
+    ALLOC_MISSING(c->lcap, AXBC_MAX_LEVELS * 4, &c->bytes);
+    ALLOC_MISSING(c->lheavy, AXBC_MAX_LEVELS * 4, &c->bytes);
+    c->tables_ready = true;
     return AXBC_OK;
 }
 
@@ -1236,33 +1240,38 @@ int axbc_batch_levels_alloc(axbc_ctx *c, int levels)
         axbc_set_error("traversal deeper than %d levels", AXBC_MAX_LEVELS - 2);
         return AXBC_ERR_RANGE;
     }
-    const size_t have = c->fmask.size();
+    // masks allocated by an earlier, partly failed call reach the device table
+    // here too: fmtab_synced counts the entries copied so far
+    int rc = AXBC_OK;
     while ((int)c->fmask.size() < levels) {
         uint32_t *p = nullptr;
-        TRY(axbc_dalloc((void **)&p, c->g->n * 4, &c->bytes));
-        CU(cudaMemset(p, 0, c->g->n * 4));
+        if ((rc = axbc_dalloc((void **)&p, c->g->n * 4, &c->bytes)) != AXBC_OK) break;
         c->fmask.push_back(p);
+        CU(cudaMemset(p, 0, c->g->n * 4));
     }
-    if (c->fmask.size() > have)
-        CU(cudaMemcpy(c->fmtab + have, c->fmask.data() + have,
-                      (c->fmask.size() - have) * sizeof(uint32_t *), cudaMemcpyHostToDevice));
-    return AXBC_OK;
+    if (c->fmask.size() > c->fmtab_synced) {
+        CU(cudaMemcpy(c->fmtab + c->fmtab_synced, c->fmask.data() + c->fmtab_synced,
+                      (c->fmask.size() - c->fmtab_synced) * sizeof(uint32_t *), cudaMemcpyHostToDevice));
+        c->fmtab_synced = c->fmask.size();
+    }
+    return rc;
 }
 
 int axbc_ensure_batch(axbc_ctx *c)
 {
-    if (c->seen) return AXBC_OK;
+    if (c->batch_ready) return AXBC_OK;
     const uint64_t n = c->g->n;
-    TRY(axbc_dalloc((void **)&c->seen, n * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->msigma, n * AXBC_W * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->mdelta, n * AXBC_W * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->mq, n * AXBC_W * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->task_ctr, 64, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->mpartial, (c->g->fwd.n_heavy_items + 1) * AXBC_W * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->bi, sizeof(BatchInfo), &c->bytes));
-    CU(cudaMallocHost((void **)&c->bi_host, sizeof(BatchInfo)));
+    ALLOC_MISSING(c->seen, n * 4, &c->bytes);
+    ALLOC_MISSING(c->msigma, n * AXBC_W * 4, &c->bytes);
+    ALLOC_MISSING(c->mdelta, n * AXBC_W * 4, &c->bytes);
+    ALLOC_MISSING(c->mq, n * AXBC_W * 4, &c->bytes);
+    ALLOC_MISSING(c->task_ctr, 64, &c->bytes);
+    ALLOC_MISSING(c->mpartial, (c->g->fwd.n_heavy_items + 1) * AXBC_W * 4, &c->bytes);
+    ALLOC_MISSING(c->bi, sizeof(BatchInfo), &c->bytes);
+    if (!c->bi_host) CU(cudaMallocHost((void **)&c->bi_host, sizeof(BatchInfo)));
     CU(cudaMemset(c->bi, 0, sizeof(BatchInfo)));
     TRY(axbc_batch_levels_alloc(c, 10));
+    c->batch_ready = true;
     return AXBC_OK;
 }
 
@@ -1366,12 +1375,16 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     c->prev_lend = 0;
     TRY(axbc_batch_settle(c));
     if (c->pool_short && c->lpool_cap < 32 * n + 64) {
+        // the larger pool is allocated before the old one goes, so a failed
+        // allocation leaves the context with a usable (smaller) pool
+        const uint32_t ncap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, 32 * n + 64),
+                                                           0xffffffffull);
+        uint32_t *np = nullptr;
+        TRY(axbc_dalloc((void **)&np, (uint64_t)ncap * 4, &c->bytes));
         CU(cudaStreamSynchronize(s));
         axbc_dfree(c->lpool);
-        c->lpool = nullptr;
-        c->lpool_cap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, 32 * n + 64),
-                                                    0xffffffffull);
-        TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)c->lpool_cap * 4, &c->bytes));
+        c->lpool = np;
+        c->lpool_cap = ncap;
         c->pool_short = false;
         if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
         if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);

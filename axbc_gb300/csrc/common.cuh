@@ -189,6 +189,10 @@ struct axbc_ctx {
     axbc_graph *g = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // lazily allocated state is complete (a failed allocation leaves it false,
+    // and the next call allocates what is still missing)
+    bool single_ready = false, batch_ready = false, tables_ready = false, sampler_ready = false;
+    size_t fmtab_synced = 0;  // level-mask pointers copied into the device table
     float *bc = nullptr;
     float *delta_last = nullptr;
     bool delta_last_valid = false;
@@ -275,6 +279,12 @@ int axbc_kron_device(int scale, int edgefactor, uint64_t seed1, uint64_t seed2, 
 // allocation with byte accounting
 int axbc_dalloc(void **p, size_t bytes, uint64_t *acct);
 void axbc_dfree(void *p);
+
+// allocate a lazily created member unless an earlier, partly failed call did
+#define ALLOC_MISSING(ptr, bytes, acct)                                               \
+    do {                                                                              \
+        if (!(ptr)) TRY(axbc_dalloc((void **)&(ptr), (bytes), (acct)));               \
+    } while (0)
 
 // a scratch device buffer freed when it goes out of scope (error paths included)
 struct DBuf {

@@ -751,46 +751,42 @@ int axbc_build_deg_dist(axbc_graph *g, cudaStream_t s)
 {
     if (g->have_deg_dist) return AXBC_OK;
     const uint64_t n = g->n;
-    uint32_t *d2 = nullptr;
-    TRY(axbc_dalloc((void **)&d2, n * 4, nullptr));
-    TRY(axbc_dalloc((void **)&g->deg2p, n * 4, &g->bytes));
-    TRY(axbc_dalloc((void **)&g->sdn, n * 4, &g->bytes));
-    k_deg2<<<1024, 256, 0, s>>>(g->fwd.col, d2, n);
+    DBuf d2, tmp, ends, cnt;
+    TRY(d2.alloc(n * 4));
+    ALLOC_MISSING(g->deg2p, n * 4, &g->bytes);
+    ALLOC_MISSING(g->sdn, n * 4, &g->bytes);
+    k_deg2<<<1024, 256, 0, s>>>(g->fwd.col, d2.as<uint32_t>(), n);
     k_sdn<<<2048, 256, 0, s>>>(g->fwd.col, g->fwd.row, g->sdn, n);
     CU_LAUNCH("deg2/sdn");
-    void *tmp = nullptr;
     size_t tb = 0;
-    cub::DeviceScan::InclusiveSum(nullptr, tb, d2, g->deg2p, (int64_t)n, s);
-    TRY(axbc_dalloc(&tmp, tb, nullptr));
-    cub::DeviceScan::InclusiveSum(tmp, tb, d2, g->deg2p, (int64_t)n, s);
+    cub::DeviceScan::InclusiveSum(nullptr, tb, d2.as<uint32_t>(), g->deg2p, (int64_t)n, s);
+    TRY(tmp.alloc(tb));
+    cub::DeviceScan::InclusiveSum(tmp.p, tb, d2.as<uint32_t>(), g->deg2p, (int64_t)n, s);
     CU_LAUNCH("deg2 scan");
-    axbc_dfree(tmp);
-    axbc_dfree(d2);
     // run ends: the prefix wraps at most (total / 2^32) + 1 times
     const uint32_t cap = 1u << 20;
-    uint32_t *ends = nullptr, *cnt = nullptr;
-    TRY(axbc_dalloc((void **)&ends, cap * 4, nullptr));
-    TRY(axbc_dalloc((void **)&cnt, 4, nullptr));
-    CU(cudaMemsetAsync(cnt, 0, 4, s));
-    k_wraps<<<1024, 256, 0, s>>>(g->deg2p, n, ends, cnt, cap);
+    TRY(ends.alloc(cap * 4));
+    TRY(cnt.alloc(4));
+    CU(cudaMemsetAsync(cnt.p, 0, 4, s));
+    k_wraps<<<1024, 256, 0, s>>>(g->deg2p, n, ends.as<uint32_t>(), cnt.as<uint32_t>(), cap);
     CU_LAUNCH("k_wraps");
     uint32_t nw = 0;
-    CU(cudaMemcpyAsync(&nw, cnt, 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(&nw, cnt.p, 4, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     if (nw > cap) {
         axbc_set_error("degree^2 prefix wraps too often");
         return AXBC_ERR_RANGE;
     }
     std::vector<uint32_t> h(nw);
-    if (nw) CU(cudaMemcpy(h.data(), ends, nw * 4, cudaMemcpyDeviceToHost));
+    if (nw) CU(cudaMemcpy(h.data(), ends.p, nw * 4, cudaMemcpyDeviceToHost));
     std::sort(h.begin(), h.end());
     h.push_back((uint32_t)n);
-    g->n_seg = (uint32_t)h.size();
+    axbc_dfree(g->seg_end);  // an earlier, failed call may have left one
+    g->seg_end = nullptr;
     TRY(axbc_dalloc((void **)&g->seg_end, h.size() * 4, &g->bytes));
+    g->n_seg = (uint32_t)h.size();
     CU(cudaMemcpy(g->seg_end, h.data(), h.size() * 4, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(&g->sum_deg, g->deg2p + n - 1, 4, cudaMemcpyDeviceToHost));
-    axbc_dfree(ends);
-    axbc_dfree(cnt);
     g->have_deg_dist = true;
     return AXBC_OK;
 }
@@ -872,21 +868,19 @@ int axbc_build_lcc(axbc_graph *g, cudaStream_t s)
 {
     if (g->have_lcc) return AXBC_OK;
     const uint64_t n = g->n;
-    uint32_t *cnt = nullptr;
-    TRY(axbc_dalloc((void **)&cnt, n * 4, nullptr));
-    TRY(axbc_dalloc((void **)&g->lcc, n * 4, &g->bytes));
-    TRY(axbc_dalloc((void **)&g->lcc_local, n * 8, &g->bytes));
-    TRY(axbc_dalloc((void **)&g->lcc_csum, ((n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK) * 8,
-                    &g->bytes));
-    CU(cudaMemsetAsync(cnt, 0, n * 4, s));
-    k_lcc_count<<<4096, 256, 0, s>>>(g->fwd, cnt);
-    k_lcc_final<<<1024, 256, 0, s>>>(g->fwd.col, cnt, g->lcc, n);
+    DBuf cnt;
+    TRY(cnt.alloc(n * 4));
+    ALLOC_MISSING(g->lcc, n * 4, &g->bytes);
+    ALLOC_MISSING(g->lcc_local, n * 8, &g->bytes);
+    ALLOC_MISSING(g->lcc_csum, ((n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK) * 8, &g->bytes);
+    CU(cudaMemsetAsync(cnt.p, 0, n * 4, s));
+    k_lcc_count<<<4096, 256, 0, s>>>(g->fwd, cnt.as<uint32_t>());
+    k_lcc_final<<<1024, 256, 0, s>>>(g->fwd.col, cnt.as<uint32_t>(), g->lcc, n);
     CU_LAUNCH("lcc");
     TRY(axbc_hprefix_launch(g->lcc, n, g->lcc_local, g->lcc_csum, s));
     const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
     CU(cudaMemcpyAsync(&g->S_lcc, g->lcc_csum + nb - 1, 8, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
-    axbc_dfree(cnt);
     g->have_lcc = true;
     return AXBC_OK;
 }

@@ -893,21 +893,28 @@ static int ensure_sampler(axbc_ctx *c, uint32_t nchecks)
 {
     const uint64_t n = c->g->n;
     TRY(axbc_ensure_batch(c));
-    if (!c->ss) {
-        TRY(axbc_dalloc((void **)&c->ss, sizeof(SamplerState), &c->bytes));
-        CU(cudaMallocHost((void **)&c->ss_host, sizeof(SamplerState)));
-        TRY(axbc_dalloc((void **)&c->used, n, &c->bytes));
+    if (!c->sampler_ready) {
+        ALLOC_MISSING(c->ss, sizeof(SamplerState), &c->bytes);
+        if (!c->ss_host) CU(cudaMallocHost((void **)&c->ss_host, sizeof(SamplerState)));
+        ALLOC_MISSING(c->used, n, &c->bytes);
         const uint64_t nb = (n + AXBC_SAMPLE_BLOCK - 1) / AXBC_SAMPLE_BLOCK;
-        TRY(axbc_dalloc((void **)&c->dyn_local, n * 8, &c->bytes));
-        TRY(axbc_dalloc((void **)&c->dyn_csum, nb * 8, &c->bytes));
-        TRY(axbc_dalloc((void **)&c->dyn_local2, n * 8, &c->bytes));
-        TRY(axbc_dalloc((void **)&c->dyn_csum2, nb * 8, &c->bytes));
+        ALLOC_MISSING(c->dyn_local, n * 8, &c->bytes);
+        ALLOC_MISSING(c->dyn_csum, nb * 8, &c->bytes);
+        ALLOC_MISSING(c->dyn_local2, n * 8, &c->bytes);
+        ALLOC_MISSING(c->dyn_csum2, nb * 8, &c->bytes);
+        c->sampler_ready = true;
     }
-    if (!c->checks || nchecks > c->nchecks_cap) {
+    if (!c->checks || !c->checkval || nchecks > c->nchecks_cap) {
+        // both new buffers first: a failure keeps the old pair
+        DBuf nc, nv;
+        TRY(nc.alloc((nchecks + 1) * 4));
+        TRY(nv.alloc((nchecks + 1) * 4));
         axbc_dfree(c->checks);
         axbc_dfree(c->checkval);
-        TRY(axbc_dalloc((void **)&c->checks, (nchecks + 1) * 4, &c->bytes));
-        TRY(axbc_dalloc((void **)&c->checkval, (nchecks + 1) * 4, &c->bytes));
+        c->checks = nc.as<uint32_t>();
+        c->checkval = nv.as<float>();
+        nc.p = nv.p = nullptr;
+        c->bytes += 2 * (uint64_t)(nchecks + 1) * 4;
         c->nchecks_cap = nchecks;
     }
     return AXBC_OK;

@@ -291,16 +291,17 @@ __global__ void k_set_root1(uint32_t v0, int level, uint32_t sig, int32_t *lvl, 
 
 int axbc_ensure_single(axbc_ctx *c)
 {
-    if (c->lvl) return AXBC_OK;
+    if (c->single_ready) return AXBC_OK;
     const uint64_t n = c->g->n;
-    TRY(axbc_dalloc((void **)&c->lvl, n * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->sigma, n * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->delta, n * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->queue, (n + 1) * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->partial, (c->g->fwd.n_heavy_items + 1) * 4, &c->bytes));
-    TRY(axbc_dalloc((void **)&c->pc, sizeof(PivotCounters), &c->bytes));
-    CU(cudaMallocHost((void **)&c->pc_host, sizeof(PivotCounters)));
+    ALLOC_MISSING(c->lvl, n * 4, &c->bytes);
+    ALLOC_MISSING(c->sigma, n * 4, &c->bytes);
+    ALLOC_MISSING(c->delta, n * 4, &c->bytes);
+    ALLOC_MISSING(c->queue, (n + 1) * 4, &c->bytes);
+    ALLOC_MISSING(c->partial, (c->g->fwd.n_heavy_items + 1) * 4, &c->bytes);
+    ALLOC_MISSING(c->pc, sizeof(PivotCounters), &c->bytes);
+    if (!c->pc_host) CU(cudaMallocHost((void **)&c->pc_host, sizeof(PivotCounters)));
     CU(cudaMemset(c->pc, 0, sizeof(PivotCounters)));
+    c->single_ready = true;
     return AXBC_OK;
 }
 
