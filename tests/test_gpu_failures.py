@@ -74,3 +74,52 @@ def _failure_loop(axbc, G, run, want, name):
         if ok:
             break
     assert failures >= 1
+
+
+def test_server_recovers_from_each_failed_allocation(axbc, golden):
+    """A device allocation made to fail at each point of adding a graph and
+    serving a request (the server's worker thread included): the call or the
+    request fails with AXBC_ERR_NOMEM, a second request on the same server gets
+    the exact result, and closing the server frees every byte."""
+    g, G = golden
+    prm = dict(z=3, nbfs=48, bader_c=0, nchecks=1, H=0, seed=9, W=8)
+    ref = axbc.Context(G)
+    ref.run_sampled(**prm)
+    want = ref.bc()
+    ref.close()
+    gc.collect()
+    gc.disable()
+    try:
+        L = axbc.lib()
+        base = L.axbc_device_bytes_live()
+        for k in range(40):
+            srv = axbc.Server()
+            L.axbc_inject_alloc_failure_after(k)
+            failed = False
+            try:
+                gid = srv.add_graph(G, H=0)
+                info = srv.wait(srv.submit(gid, **prm), timeout_ms=60000)
+                if info["state"] == "failed":
+                    assert info["status"] == 3, info
+                    failed = True
+                else:
+                    assert info["state"] == "done", info
+            except axbc.AxbcError as ex:
+                assert ex.status == 3, ex
+                failed = True
+                gid = None
+            finally:
+                L.axbc_inject_alloc_failure_after(-1)
+            if gid is None:
+                gid = srv.add_graph(G, H=0)
+            rid = srv.submit(gid, **prm)
+            info = srv.wait(rid, timeout_ms=60000)
+            assert info["state"] == "done", (k, info)
+            bc, _, _ = srv.result(rid, G.n)
+            same_bits(bc, want, f"server, failure after {k} allocations")
+            srv.close()
+            assert L.axbc_device_bytes_live() == base, f"server: leak after failing allocation {k}"
+            if not failed:
+                break
+    finally:
+        gc.enable()
