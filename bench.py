@@ -377,7 +377,7 @@ def main():
     avg_s = ms / max(cnt, 1) / 1000.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-                "model": "survey 8d traversed-edge bytes: (4/W+8) B/TE backward, (4/W+4) "
+                "model": "traversed-edge bytes, Graph500 counting: (4/W+8) B/TE backward, (4/W+4) "
                          "forward; counts every edge of a reached vertex",
                 "dram_gbs_from_traffic": (traffic / avg_s / 1e9) if traffic else None,
                 "dram_frac_from_traffic": (traffic / avg_s / 1e9 / peak) if traffic else None,
