@@ -166,6 +166,16 @@ def oracle_sample(g_csc, pivots, probs, seconds, threads):
     return te / dt, k, dt
 
 
+def oracle_single(g_csc, pivots, probs):
+    """The oracle on one thread over a few pivots: (TE/s, seconds)."""
+    import oracle
+    g = oracle.CSC(*g_csc)
+    t0 = time.perf_counter()
+    _, _, te = oracle.bc_pivots(g, pivots, probs, 0)
+    dt = time.perf_counter() - t0
+    return te / dt, dt
+
+
 def serve_bench(args):
     """The request server under Poisson arrivals (seed 11) over resident graphs:
     Kronecker scales 16, 18, 20, 22 (edgefactor 16) and a 1024x1024 grid.  Each
@@ -452,9 +462,12 @@ def main():
         csc = G.csc()
         threads = cpu_threads()
         v, k, dt = oracle_sample(csc, piv, pr, args.cpu_seconds, threads)
+        v1, dt1 = oracle_single(csc, piv[:1], pr[:1])
         out["cpu_baseline"] = {"value": v, "unit": "TE/s", "cores": threads, "kind": "port",
                                "sample": f"{k} pivots of the step's pivot list in {dt:.1f} s, "
-                                         "OpenMP over pivots (oracle/ C restatement)"}
+                                         "OpenMP over pivots (oracle/ C restatement)",
+                               "single_thread": {"value": v1, "unit": "TE/s", "cores": 1,
+                                                 "sample": f"the first pivot of the list in {dt1:.1f} s"}}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
