@@ -46,17 +46,20 @@ def test_cli_output_and_accuracy_report(axbc, tmp_path):
     assert np.array_equal(v1, ve)
 
 
-@pytest.mark.parametrize("opts,H,z,nbfs,W", [
-    (("-N", "96", "-z", "1", "-c", "0", "-H", "1", "-W", "64"), 1, 1, 96, 64),
-    (("-N", "200", "-z", "5", "-c", "0"), 0, 5, 200, 1),
+@pytest.mark.parametrize("opts,H,z,nbfs,W,undirected", [
+    (("-N", "96", "-z", "1", "-c", "0", "-H", "1", "-W", "64"), 1, 1, 96, 64, True),
+    (("-N", "200", "-z", "5", "-c", "0"), 0, 5, 200, 1, True),
+    (("-N", "64", "-z", "0", "-c", "0", "-U", "-W", "32"), 0, 0, 64, 32, False),
 ])
-def test_cli_output_file_equals_the_reference_definition(axbc, orc, tmp_path, opts, H, z, nbfs, W):
+def test_cli_output_file_equals_the_reference_definition(axbc, orc, tmp_path, opts, H, z, nbfs, W,
+                                                         undirected):
     """The reference's command line on its own generated input (-S 10 -E 16:
-    the Graph500 generator, seeds 23/24): the output file is the oracle's run
-    on the reference pipeline's graph, printed as bc/2/nrounds with "%d\\t%.2f"."""
-    path, _ = run_cli(axbc, tmp_path, f"ref{z}", *opts)
+    the Graph500 generator, seeds 23/24; -U keeps its pairs directed): the
+    output file is the oracle's run on the reference pipeline's graph, printed
+    as bc/2/nrounds with "%d\\t%.2f"."""
+    path, _ = run_cli(axbc, tmp_path, f"ref{z}{int(undirected)}", *opts)
     e = orc.kron_edges(10, 16).astype(np.uint64)
-    g = orc.pipeline(e, 1024, True, H)
+    g = orc.pipeline(e, 1024, undirected, H)
     want = orc.run(g, z=z, nbfs=nbfs, bader_c=0, nchecks=1, H=H, seed=4343543, W=W)
     bc = want["bc"].astype(np.float32)
     lines = [f"{k}\t{float(bc[k]) / 2.0 / want['nrounds']:.2f}\n" for k in range(1024)]
