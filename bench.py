@@ -46,8 +46,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no e2e pass")
     ap.add_argument("--skip-plain", action="store_true", help="profiling runs: no plain pass")
-    ap.add_argument("--workload", default="headline", choices=["headline", "serving"],
-                    help="serving: the request server on resident graphs (p50/p99 latency)")
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "serving", "config1", "config2", "config3"],
+                    help="serving: the request server on resident graphs (p50/p99 latency); "
+                         "config1..3: the other benchmark configurations, one sampled run "
+                         "per step, with the oracle on the host beside it")
     ap.add_argument("--requests", type=int, default=48, help="serving: requests submitted")
     ap.add_argument("--rate", type=float, default=2.0, help="serving: mean arrivals per second")
     ap.add_argument("--push-factor", type=float, default=None,
@@ -176,6 +179,92 @@ def oracle_single(g_csc, pivots, probs):
     return te / dt, dt
 
 
+# The other benchmark configurations: graph, heuristic, budget, stop rule, width
+# (None: from the autotuner), one-degree reduction.
+CONFIGS = {
+    "config1": dict(graph=("kron", 14), H=0, z=0, nbfs=256, c=0, x=1, seed=1, W=32,
+                    desc="Kronecker scale 14 (Graph500 generator, seeds 23/24), -H 0 -z 0 -N 256 -c 0"),
+    "config2": dict(graph=("kron", 20), H=1, z=1, nbfs=4096, c=0, x=1, seed=1, W=64,
+                    desc="Kronecker scale 20, -H 1 -z 1 -N 4096 -c 0, width 64"),
+    "config3": dict(graph=("grid", 2048), H=0, z=4, nbfs=2048, c=1, x=8, seed=1, W=None,
+                    desc="2048x2048 grid (2% edges dropped, seed 7; 0.01% long-range), "
+                         "-z 4 -N 2048 -c 1 -x 8, width from the autotuner"),
+}
+
+
+def config_bench(args):
+    """One of the other benchmark configurations: each step is one whole
+    sampled run on the GPU (CUDA events on the context's stream); the oracle
+    times the same run's pivots on the host (OpenMP over pivots), all of them
+    when that fits the CPU budget, else a sample scaled per pivot."""
+    import numpy as np
+    import torch
+    import axbc_gb300 as ax
+    cf = CONFIGS[args.workload]
+    torch.cuda.init()
+    kind, size = cf["graph"]
+    t_graph = time.perf_counter()
+    G = ax.Graph.kronecker(size, 16, 23, 24, H=cf["H"]) if kind == "kron" else \
+        ax.Graph.grid(size, 0.02, 1e-4, seed=7)
+    build_s = time.perf_counter() - t_graph
+    stream = torch.cuda.Stream()
+    ctx = ax.Context(G, stream=stream.cuda_stream)
+    W = cf["W"]
+    if W is None:
+        deg = G.deg()
+        rng = np.random.default_rng(1234)
+        trial = rng.choice(np.flatnonzero(deg > 0), size=64, replace=False).astype(np.uint32)
+        W = int(ctx.autotune(trial)["batch_width"])
+
+    def run():
+        ctx.reset()
+        return ctx.run_sampled(z=cf["z"], nbfs=cf["nbfs"], bader_c=cf["c"], nchecks=cf["x"], H=cf["H"],
+                               seed=cf["seed"], W=W)
+
+    for _ in range(max(1, args.warmup)):
+        r = run()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    te = 0
+    for _ in range(args.steps):
+        r = run()
+        te += r["te"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t = ev0.elapsed_time(ev1) / 1000.0
+    out = {"metric": "BC traversed-edges/s (fwd+bwd)", "value": te / t, "unit": "TE/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000 / args.steps,
+           "higher_is_better": True, "impl": "gb300", "workload": args.workload,
+           "config": {"workload": cf["desc"], "batch_width": W, "graph_build_s": round(build_s, 3),
+                      "n": G.n, "m": G.m},
+           "rounds": int(r["nrounds"]), "stopped": bool(r["stopped"]), "te_per_run": int(r["te"])}
+    if not args.no_cpu_baseline:
+        col, row, reach = G.csc()
+        piv, pr = r["pivots"], r["probs"]
+        threads = cpu_threads()
+        import oracle
+        oracle.build()
+        g = oracle.CSC(col, row, reach)
+        # the whole pivot list when a first chunk says it fits the budget
+        k0 = min(len(piv), threads)
+        t0 = time.perf_counter()
+        _, te0 = oracle.bc_pivots_omp(g, piv[:k0], pr[:k0], cf["H"], threads)
+        dt0 = time.perf_counter() - t0
+        per_pivot = dt0 / max(k0, 1)
+        if per_pivot * len(piv) <= args.cpu_seconds * 4:
+            t0 = time.perf_counter()
+            _, te_all = oracle.bc_pivots_omp(g, piv, pr, cf["H"], threads)
+            dt = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": te_all / dt, "unit": "TE/s", "cores": threads, "kind": "port",
+                                   "sample": f"all {len(piv)} pivots of the run in {dt:.1f} s"}
+        else:
+            out["cpu_baseline"] = {"value": te0 / dt0, "unit": "TE/s", "cores": threads, "kind": "port",
+                                   "sample": f"{k0} of the run's {len(piv)} pivots in {dt0:.1f} s "
+                                             f"(whole run extrapolated: {per_pivot * len(piv):.0f} s)"}
+    print(json.dumps(out), flush=True)
+
+
 def serve_bench(args):
     """The request server under Poisson arrivals (seed 11) over resident graphs:
     Kronecker scales 16, 18, 20, 22 (edgefactor 16) and a 1024x1024 grid.  Each
@@ -253,6 +342,8 @@ def main():
     args = parse()
     if args.workload == "serving":
         return serve_bench(args)
+    if args.workload in CONFIGS:
+        return config_bench(args)
     from axbc_gb300 import sharding
     rank, world, local = sharding.env()
     import numpy as np
