@@ -258,8 +258,8 @@ struct axbc_ctx {
     double level_te_prev = 0;  // degree sum of the previous level's new vertices
     std::vector<double> level_te;
     // tuning
-    double push_factor_single = 1.0;
-    double push_factor_batch = 1.0;
+    double push_factor_single = 8.0;  // defaults: see axbc_ctx_set_tuning
+    double push_factor_batch = 8.0;
     uint64_t bytes = 0;
     int num_sms = 0;
     int dyn_blocks_per_sm = 0;  // resident blocks of the dynamic kernels

@@ -29,6 +29,10 @@ def main():
     ap.add_argument("--width", type=int, default=32)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--profile", action="store_true", help="time every kernel with CUDA events")
+    ap.add_argument("--push-factor", type=float, default=None,
+                    help="batched push/pull factor (default: the library's)")
+    ap.add_argument("--levels", action="store_true",
+                    help="with --profile: per forward level / backward depth times (ms, > 0.005)")
     a = ap.parse_args()
     import axbc_gb300 as ax
     kind, size = a.graph.split(":")
@@ -41,6 +45,8 @@ def main():
     else:
         raise SystemExit(f"unknown graph kind {kind!r}")
     ctx = ax.Context(G)
+    if a.push_factor is not None:
+        ctx.set_tuning(32.0, a.push_factor)
     deg = G.deg()
     rng = np.random.default_rng(a.seed)
     cand = np.flatnonzero(deg > 0)
@@ -51,13 +57,20 @@ def main():
         st = ctx.run_batch(piv, np.full(a.width, 1.0 / G.n))
         ctx.sync()
         dt = time.perf_counter() - t0
+        per_level = {}
+        if a.profile and a.levels:
+            for kind, tag, ms, _ in ctx.profile_records():
+                if tag >= 0 and ms > 0.005:
+                    key = f"{kind}@{tag}"
+                    per_level[key] = round(per_level.get(key, 0.0) + ms, 3)
         pr = ctx.profile_read() if a.profile else {}
         ls = ctx.level_stats()
         print(json.dumps({
             "batch": b, "graph": a.graph, "n": G.n, "s": round(dt, 5),
             "levels": int(max(s["levels"] for s in st)), "te": int(sum(s["te"] for s in st)),
             "overflow_levels": int(np.sum(ls["list_count"] > ls["list_cap"])),
-            "kernel_ms": {k: round(v[0], 3) for k, v in pr.items() if v[1]}}), flush=True)
+            "kernel_ms": {k: round(v[0], 3) for k, v in pr.items() if v[1]},
+            **({"level_ms": per_level} if per_level else {})}), flush=True)
 
 
 if __name__ == "__main__":
