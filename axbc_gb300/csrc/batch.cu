@@ -1317,7 +1317,7 @@ static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
                                              ll, c->lpool_cap, list_max_of(c));
 }
 
-static void bwd_step_kernels(axbc_ctx *c, int dgrid)
+static void bwd_step_kernels(axbc_ctx *c)
 {
     axbc_graph *g = c->g;
     k_bwd_step<<<bwd_grid(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
@@ -1339,7 +1339,7 @@ static int capture_steps(axbc_ctx *c, int dgrid, int sgrid)
         cudaGraph_t gr = nullptr;
         CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         if (which == 0) fwd_step_kernels(c, dgrid, sgrid);
-        else bwd_step_kernels(c, dgrid);
+        else bwd_step_kernels(c);
         cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
         if (e != cudaSuccess) return axbc_cuda_fail(e, "capture level step", __FILE__, __LINE__);
         e = cudaGraphInstantiate(which == 0 ? &c->fwd_step_exec : &c->bwd_step_exec, gr, 0);
