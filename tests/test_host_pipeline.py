@@ -61,3 +61,37 @@ def test_read_edge_file(axbc, tmp_path):
     bad.write_text("0 1\n7 2\n")
     with pytest.raises(axbc.AxbcError):
         axbc.read_edge_file(str(bad), 6)
+
+
+def _adversarial(rng):
+    """Random multigraph with the structures the one-degree reduction treats
+    specially: isolated edges, stars, self-loops (one on vertex 0, which sorts
+    first), repeated edges, a leaf on the largest id."""
+    n = int(rng.integers(2, 400))
+    parts = [rng.integers(0, n, size=(int(rng.integers(0, 3 * n)), 2))]
+    for _ in range(int(rng.integers(0, 6))):
+        parts.append(rng.integers(0, n, size=(1, 2)))
+    for _ in range(int(rng.integers(0, 4))):
+        hub = rng.integers(0, n)
+        leaves = rng.integers(0, n, size=int(rng.integers(1, 20)))
+        parts.append(np.stack([np.full(len(leaves), hub), leaves], 1))
+    if rng.random() < 0.5:
+        loops = rng.integers(0, n, size=int(rng.integers(1, 5)))
+        parts.append(np.stack([loops, loops], 1))
+        parts.append(np.array([[0, 0]]))
+    if rng.random() < 0.5:
+        parts.append(np.array([[n - 1, int(rng.integers(0, n))]]))
+    e = np.concatenate(parts).astype(np.uint64)
+    e = e[rng.permutation(len(e))]
+    if rng.random() < 0.3:
+        e = np.concatenate([e, e[: len(e) // 3]])
+    return e, n
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_adversarial_multigraphs(axbc, orc, seed):
+    rng = np.random.default_rng(9000 + seed)
+    e, n = _adversarial(rng)
+    undirected = bool(rng.random() < 0.8)
+    H = int(rng.random() < 0.6)
+    _same(axbc, orc, e, n, undirected, H)
