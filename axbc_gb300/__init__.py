@@ -115,6 +115,8 @@ _SIGS = {
     "axbc_ctx_profile": (C.c_int, [_P, C.c_int]),
     "axbc_ctx_profile_read": (C.c_int, [_P, _P, _P, _P, C.c_int]),
     "axbc_ctx_launches": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "axbc_ctx_count": (C.c_int, [_P, C.c_int]),
+    "axbc_ctx_count_read": (C.c_int, [_P, _P, C.c_int]),
     "axbc_autotune": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(Tuning)]),
     "axbc_bc_pivot_static": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_uint64, C.c_uint32,
                                        C.c_double, C.c_int, _P, _P, C.POINTER(PivotStats)]),
@@ -146,6 +148,8 @@ _SIGS = {
 PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bwd",
               "batch_bwd_combine", "batch_update", "sampler", "plain_fwd", "plain_bwd",
               "plain_other"]
+# work counters per kind (axbc_ctx_count_read)
+WORK_FIELDS = ["bytes", "entries", "gathers", "pairs"]
 # kernel names behind each profiling kind (for matching ncu launch lists)
 PROF_KERNELS = {"batch_fwd_push": "k_fwd_push_step", "batch_fwd_pull": "k_fwd_pull_step",
                 "batch_level_stats": "k_stats_step", "batch_bwd": "k_bwd_step",
@@ -405,7 +409,7 @@ class Context:
         _check(lib().axbc_ctx_sync(self._h))
 
     def autotune(self, pivots, H=0):
-        """Pick direction-switch factors and batch width on these pivots (resets bc)."""
+        """Pick direction-switch factors and batch width on these pivots (bc is kept)."""
         v = np.ascontiguousarray(pivots, dtype=np.uint32)
         t = Tuning()
         _check(lib().axbc_autotune(self._h, _ptr(v), len(v), H, C.byref(t)))
@@ -468,6 +472,20 @@ class Context:
         by = np.zeros(k, np.float64)
         _check(lib().axbc_ctx_profile_read(self._h, _ptr(ms), _ptr(cnt), _ptr(by), k))
         return {PROF_KINDS[i]: (float(ms[i]), int(cnt[i]), float(by[i])) for i in range(k)}
+
+    def count(self, enable=True):
+        """Run the counting builds of the traversal kernels (measurement only)."""
+        _check(lib().axbc_ctx_count(self._h, int(enable)))
+
+    def count_read(self):
+        """{kind: {bytes, entries, gathers, pairs}} since count() / the last read:
+        the bytes each kind of launch must move at least and the work behind them."""
+        k = len(PROF_KINDS)
+        out = np.zeros(k * WORK_FIELDS.__len__(), np.uint64)
+        _check(lib().axbc_ctx_count_read(self._h, _ptr(out), k))
+        out = out.reshape(k, len(WORK_FIELDS))
+        return {PROF_KINDS[i]: {f: int(out[i, j]) for j, f in enumerate(WORK_FIELDS)}
+                for i in range(k) if out[i].any()}
 
     @property
     def launches(self):

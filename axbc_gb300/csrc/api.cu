@@ -146,6 +146,32 @@ extern "C" int axbc_ctx_profile_records(axbc_ctx *c, int32_t *kinds, int32_t *ta
     return AXBC_OK;
 }
 
+extern "C" int axbc_ctx_count(axbc_ctx *c, int enable)
+{
+    CHECK_ARG(c, "axbc_ctx_count: null context");
+    CU(cudaStreamSynchronize(c->stream));
+    if (enable && !c->wcount) {
+        TRY(axbc_dalloc((void **)&c->wcount, KP_NKINDS * WC_NFIELDS * 8, &c->bytes));
+        CU(cudaMemset(c->wcount, 0, KP_NKINDS * WC_NFIELDS * 8));
+    }
+    c->count_on = enable != 0;
+    return AXBC_OK;
+}
+
+extern "C" int axbc_ctx_count_read(axbc_ctx *c, uint64_t *counts, int nkinds)
+{
+    CHECK_ARG(c && counts, "axbc_ctx_count_read: null argument");
+    CHECK_ARG(nkinds >= 0 && nkinds <= KP_NKINDS, "axbc_ctx_count_read: nkinds out of range");
+    for (int i = 0; i < nkinds * WC_NFIELDS; i++) counts[i] = 0;
+    if (!c->wcount) return AXBC_OK;
+    CU(cudaStreamSynchronize(c->stream));
+    unsigned long long h[KP_NKINDS * WC_NFIELDS];
+    CU(cudaMemcpy(h, c->wcount, sizeof(h), cudaMemcpyDeviceToHost));
+    CU(cudaMemset(c->wcount, 0, sizeof(h)));
+    for (int i = 0; i < nkinds * WC_NFIELDS; i++) counts[i] = h[i];
+    return AXBC_OK;
+}
+
 extern "C" int axbc_ctx_launches(const axbc_ctx *c, uint64_t *launches)
 {
     CHECK_ARG(c && launches, "axbc_ctx_launches: null argument");
@@ -186,6 +212,7 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     axbc_dfree(c->bc);
     axbc_dfree(c->delta_last);
+    axbc_dfree(c->wcount);
     axbc_dfree(c->lvl);
     axbc_dfree(c->sigma);
     axbc_dfree(c->delta);

@@ -200,21 +200,26 @@ __device__ __forceinline__ const uint32_t *level_list(const LevelLists &ll, int 
 // Forward level L, push from the vertices of depth L-1: for each neighbour u
 // and each pivot s with v at depth L-1 and u unseen, sigma_s[u] += sigma_s[v]
 // and bit s joins u's level-L mask.  Atomics are fire-and-forget reductions.
+template <class WC>
 __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, uint32_t b0,
                                           uint32_t b1, const uint32_t *__restrict__ seen,
                                           uint32_t *fcur, uint32_t *msigma, const LevelLists &ll,
-                                          int L)
+                                          int L, WC &wc)
 {
     const unsigned lane = lane_id();
     const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
+    if ((f >> lane) & 1u) wc.add(WC_BYTES, 4);
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
         uint32_t u = 0, nm = 0;
         if (e < b1) {
             u = a.row[e];
             nm = f & ~seen[u];
+            wc.add(WC_ENTRIES, 1);
+            wc.add(WC_BYTES, 8);  // adjacency entry, seen mask
         }
         const uint32_t old = nm ? atomicOr(&fcur[u], nm) : 1u;
+        if (nm) wc.add(WC_BYTES, old == 0u ? 8 : 4);  // level mask, list entry
         list_append(ll, L, old == 0u, u);
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
@@ -222,7 +227,11 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
             act &= act - 1;
             const uint32_t uj = __shfl_sync(FULL_MASK, u, j);
             const uint32_t mj = __shfl_sync(FULL_MASK, nm, j);
-            if ((mj >> lane) & 1u) atomicAdd(&msigma[row_base(uj) + lane], sig);
+            if ((mj >> lane) & 1u) {
+                atomicAdd(&msigma[row_base(uj) + lane], sig);
+                wc.add(WC_PAIRS, 1);
+                wc.add(WC_BYTES, 4);
+            }
         }
     }
 }
@@ -232,15 +241,17 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
 // lists 32 positions at a time, so a chunk of low-degree vertices costs one
 // pass instead of one pass per vertex.  Lane e finds its vertex by a binary
 // search over the inclusive degree prefix held across the lanes.
+template <class WC>
 __device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, uint32_t f_l,
                                              const uint32_t *__restrict__ seen, uint32_t *fcur,
-                                             uint32_t *msigma, const LevelLists &ll, int L)
+                                             uint32_t *msigma, const LevelLists &ll, int L, WC &wc)
 {
     const unsigned lane = lane_id();
     uint32_t b = 0, d = 0;
     if (f_l) {
         b = a.col[v_l];
         d = a.col[v_l + 1] - b;
+        wc.add(WC_BYTES, 8);  // adjacency bounds
     }
     uint32_t inc = d;
 #pragma unroll
@@ -262,8 +273,11 @@ __device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, uint32_
         if (e < total) {
             u = a.row[pk];
             nm = fk & ~seen[u];
+            wc.add(WC_ENTRIES, 1);
+            wc.add(WC_BYTES, 8);  // adjacency entry, seen mask
         }
         const uint32_t old = nm ? atomicOr(&fcur[u], nm) : 1u;
+        if (nm) wc.add(WC_BYTES, old == 0u ? 8 : 4);  // level mask, list entry
         list_append(ll, L, old == 0u, u);
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
@@ -281,15 +295,21 @@ __device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, uint32_
             }
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if ((mm[q] >> lane) & 1u) atomicAdd(&msigma[row_base(uu[q]) + lane], sg[q]);
+                if ((mm[q] >> lane) & 1u) {
+                    atomicAdd(&msigma[row_base(uu[q]) + lane], sg[q]);
+                    wc.add(WC_GATHERS, 1);
+                    wc.add(WC_PAIRS, 1);
+                    wc.add(WC_BYTES, 8);  // parent's path count, child's sum
+                }
         }
     }
 }
 
+template <class WC>
 __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__restrict__ fprev,
                                               uint32_t *fcur, const uint32_t *__restrict__ seen,
                                               uint32_t *msigma, uint32_t *ctr, const LevelLists &ll,
-                                              int L)
+                                              int L, WC &wc)
 {
     const unsigned lane = lane_id();
     uint32_t lcnt = 0;
@@ -305,9 +325,10 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
         if (t < nhi) {
             const uint32_t v = a.hitem_v[t];
             const uint32_t f = fprev[v];
+            if (lane == 0) wc.add(WC_BYTES, 4);
             if (!f) continue;
             const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
-            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma, ll, L);
+            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma, ll, L, wc);
             continue;
         }
         if (lst) {
@@ -316,8 +337,9 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
             if (lane < ent && i < lcnt) {
                 v_l = lst[i];
                 if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fprev[v_l];
+                wc.add(WC_BYTES, 8);  // list entry, level mask
             }
-            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L);
+            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L, wc);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
@@ -327,8 +349,9 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
             if (lane < cnt) {
                 v_l = a.order[beg + lane];
                 f_l = fprev[v_l];
+                wc.add(WC_BYTES, 4);  // level mask
             }
-            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L);
+            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L, wc);
         }
     }
 }
@@ -338,10 +361,11 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
 // any order gives the same bits).  The positions of a 32-wide chunk are staged
 // in shared memory; each 8-position group with a hit issues its eight gathers
 // before any is consumed.
+template <class WC>
 __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32_t b0, uint32_t b1,
                                               const uint32_t *__restrict__ fprev,
                                               const uint32_t *__restrict__ msigma, uint32_t *su,
-                                              uint32_t *sg, uint32_t &acc)
+                                              uint32_t *sg, uint32_t &acc, WC &wc)
 {
     const unsigned lane = lane_id();
     const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
@@ -355,6 +379,11 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
         const uint32_t v = vn;
         vn = e + 32 < b1 ? rv.row[e + 32] : 0u;
         const uint32_t fm = e < b1 ? fprev[v] & ns : 0u;
+        if (e < b1) {
+            wc.add(WC_ENTRIES, 1);
+            wc.add(WC_GATHERS, __popc(fm));
+            wc.add(WC_BYTES, 8 + 4 * __popc(fm));  // adjacency entry, level mask, parents' counts
+        }
         const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
         found |= __reduce_or_sync(FULL_MASK, fm);
@@ -388,15 +417,17 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
 // held across the lanes.  Positions arrive grouped by vertex, so one running
 // sum per lane (pivot) is written out whenever the vertex changes.  Returns the
 // discovered mask of the lane's own vertex.
+template <class WC>
 __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, uint32_t ns_l,
                                                  const uint32_t *__restrict__ fprev, uint32_t *msigma,
-                                                 uint32_t *su, uint32_t *sg, uint32_t *sk)
+                                                 uint32_t *su, uint32_t *sg, uint32_t *sk, WC &wc)
 {
     const unsigned lane = lane_id();
     uint32_t b = 0, d = 0;
     if (ns_l) {
         b = rv.col[u_l];
         d = rv.col[u_l + 1] - b;
+        wc.add(WC_BYTES, 8);  // adjacency bounds
     }
     uint32_t inc = d;
 #pragma unroll
@@ -420,6 +451,9 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
         if (e < total) {
             v = rv.row[pk];
             fm = fprev[v] & nk;
+            wc.add(WC_ENTRIES, 1);
+            wc.add(WC_GATHERS, __popc(fm));
+            wc.add(WC_BYTES, 8 + 4 * __popc(fm));  // adjacency entry, level mask, parents' counts
         }
         const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
@@ -490,11 +524,12 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
     return mine;
 }
 
+template <class WC>
 __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
                                               const uint32_t *__restrict__ fprev, uint32_t *fcur,
                                               const uint32_t *__restrict__ seen, uint32_t *msigma,
                                               uint32_t *ctr, uint32_t *su, uint32_t *sg,
-                                              uint32_t *sk, const LevelLists &ll, int L)
+                                              uint32_t *sk, const LevelLists &ll, int L, WC &wc)
 {
     const unsigned lane = lane_id();
     const uint64_t nhi = rv.n_heavy_items, nu = n_units(rv);
@@ -505,14 +540,20 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
         if (t < nhi) {
             const uint32_t u = rv.hitem_v[t];
             const uint32_t ns = srcmask & ~seen[u];
+            if (lane == 0) wc.add(WC_BYTES, 4);  // seen mask
             if (!ns) continue;
             const uint32_t b0 = rv.col[u] + rv.hitem_k[t] * AXBC_SPAN;
             uint32_t acc;
             const uint32_t nm =
-                pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg, acc);
-            if ((nm >> lane) & 1u) atomicAdd(&msigma[row_base(u) + lane], acc);
+                pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg, acc, wc);
+            if ((nm >> lane) & 1u) {
+                atomicAdd(&msigma[row_base(u) + lane], acc);
+                wc.add(WC_PAIRS, 1);
+                wc.add(WC_BYTES, 4);
+            }
             bool first = false;
             if (lane == 0 && nm) first = atomicOr(&fcur[u], nm) == 0u;
+            if (lane == 0 && nm) wc.add(WC_BYTES, first ? 8 : 4);  // level mask, list entry
             list_append(ll, L, first, u);
             continue;
         }
@@ -523,9 +564,14 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
             if (lane < cnt) {
                 u_l = rv.order[beg + lane];
                 ns_l = srcmask & ~seen[u_l];
+                wc.add(WC_BYTES, 4);  // seen mask
             }
-            const uint32_t mine = pull_light32(rv, u_l, ns_l, fprev, msigma, su, sg, sk);
-            if (mine) fcur[u_l] = mine;
+            const uint32_t mine = pull_light32(rv, u_l, ns_l, fprev, msigma, su, sg, sk, wc);
+            if (mine) {
+                fcur[u_l] = mine;
+                wc.add(WC_PAIRS, __popc(mine));
+                wc.add(WC_BYTES, 8 + 4 * __popc(mine));  // level mask, list entry, path counts
+            }
             list_append(ll, L, mine != 0u, u_l);
         }
     }
@@ -535,22 +581,27 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
 // bi->push_next (set by the previous k_level_advance).  Both direction kernels
 // are launched every level; the one not chosen returns at once, as both do
 // once a level discovered nothing.
+// CNT: the counting build (work counts into wc[KP_FWD_PUSH / KP_FWD_PULL]).
+template <bool CNT>
 __global__ void __launch_bounds__(BATCH_TPB, 8) k_fwd_push_step(Adj a, const BatchInfo *__restrict__ bi,
                                                              uint32_t *const *__restrict__ tab,
                                                              const uint32_t *__restrict__ seen,
                                                              uint32_t *msigma, uint32_t *ctrs,
-                                                             LevelLists ll)
+                                                             LevelLists ll, unsigned long long *wc)
 {
     if (!bi->alive || !bi->push_next) return;
     const int L = bi->cur + 1;
-    fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L);
+    WorkCount<CNT> cnt;
+    fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L, cnt);
+    cnt.flush(wc);
 }
 
+template <bool CNT>
 __global__ void __launch_bounds__(BATCH_TPB, AXBC_PULL_MIN_BLOCKS) k_fwd_pull_step(Adj rv, const BatchInfo *__restrict__ bi,
                                                              uint32_t *const *__restrict__ tab,
                                                              const uint32_t *__restrict__ seen,
                                                              uint32_t *msigma, uint32_t *ctrs,
-                                                             LevelLists ll)
+                                                             LevelLists ll, unsigned long long *wc)
 {
     __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
     __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
@@ -558,8 +609,10 @@ __global__ void __launch_bounds__(BATCH_TPB, AXBC_PULL_MIN_BLOCKS) k_fwd_pull_st
     if (!bi->alive || bi->push_next) return;
     const int L = bi->cur + 1;
     const unsigned w0 = threadIdx.x & ~31u;
+    WorkCount<CNT> cnt;
     fwd_pull_body(rv, bi->srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, s_u + w0, s_g + w0,
-                  s_k + w0, ll, L);
+                  s_k + w0, ll, L, cnt);
+    cnt.flush(wc);
 }
 
 // After level L = bi->cur + 1: fold the level mask into `seen` and count, per
@@ -736,9 +789,11 @@ __device__ __forceinline__ float tree8(const uint4 *su4, const uint4 *sg4, int g
 // chunk form four 8-position subtrees of the canonical tree; a subtree without
 // successors sums to +0 and is skipped.
 // `un` holds the adjacency entries of the first chunk (row[b0 + lane]).
+template <class WC>
 __device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float sv, uint32_t b0,
                                                uint32_t b1, uint32_t un, const uint32_t *__restrict__ fnext,
-                                               const float *__restrict__ mq, uint32_t *su, uint32_t *sg)
+                                               const float *__restrict__ mq, uint32_t *su, uint32_t *sg,
+                                               WC &wc)
 {
     const unsigned lane = lane_id();
     const uint32_t lanebit = 1u << lane;
@@ -752,6 +807,11 @@ __device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float s
         const uint32_t u = un;
         un = e + 32 < b1 ? a.row[e + 32] : 0u;
         const uint32_t gm = e < b1 ? fnext[u] & f : 0u;
+        if (e < b1) {
+            wc.add(WC_ENTRIES, 1);
+            wc.add(WC_GATHERS, __popc(gm));
+            wc.add(WC_BYTES, 8 + 4 * __popc(gm));  // adjacency entry, level mask, successors' q
+        }
         const unsigned pm = __ballot_sync(FULL_MASK, gm != 0);
         if (!pm) continue;
         su[lane] = u;
@@ -768,12 +828,13 @@ __device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float s
     return P;
 }
 
+template <class WC>
 __device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, uint32_t b0,
                                           uint32_t b1, const uint32_t *__restrict__ fnext,
-                                          const float *__restrict__ mq, uint32_t *su, uint32_t *sg)
+                                          const float *__restrict__ mq, uint32_t *su, uint32_t *sg, WC &wc)
 {
     const uint32_t e = b0 + lane_id();
-    return dep_span_from(a, f, sv, b0, b1, e < b1 ? a.row[e] : 0u, fnext, mq, su, sg);
+    return dep_span_from(a, f, sv, b0, b1, e < b1 ? a.row[e] : 0u, fnext, mq, su, sg, wc);
 }
 
 // delta and q of vertex v for the pivots in f
@@ -789,15 +850,22 @@ __device__ __forceinline__ void write_dep(float *mdelta, float *mq, uint32_t v, 
 
 // Backward depth d for the pivots in dmask.  With no_succ (the deepest depth)
 // nothing lies below, so delta = reach.
+template <class WC>
 __device__ __forceinline__ void bwd_vertices(const Adj &a, uint32_t v_l, uint32_t f_l, int no_succ,
                                              const uint32_t *__restrict__ fnext,
                                              const uint32_t *__restrict__ msigma, float *mdelta,
                                              float *mq, const uint32_t *__restrict__ reach,
-                                             uint32_t *su, uint32_t *sg)
+                                             uint32_t *su, uint32_t *sg, WC &wc)
 {
     const unsigned lane = lane_id();
     unsigned act = __ballot_sync(FULL_MASK, f_l != 0);
     if (!act) return;
+    // adjacency bounds and reach of each vertex; per pivot its path count
+    // read, its dependency and q written
+    if (f_l) {
+        wc.add(WC_BYTES, (no_succ ? 4 : 12) + 12 * __popc(f_l));
+        wc.add(WC_PAIRS, __popc(f_l));
+    }
     // the adjacency bounds of all listed vertices load at once; the first
     // chunk of the next vertex's adjacency loads while a vertex is summed
     uint32_t c0_l = 0, c1_l = 0;
@@ -821,13 +889,14 @@ __device__ __forceinline__ void bwd_vertices(const Adj &a, uint32_t v_l, uint32_
         }
         const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
         float P = 0.0f;
-        if (!no_succ) P = dep_span_from(a, f, __uint2float_rn(sig), cb0, cb1, cu, fnext, mq, su, sg);
+        if (!no_succ) P = dep_span_from(a, f, __uint2float_rn(sig), cb0, cb1, cu, fnext, mq, su, sg, wc);
         write_dep(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
         if (jn < 0) break;
         j = jn;
     }
 }
 
+template <class WC>
 __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_succ,
                                          const uint32_t *__restrict__ fd,
                                          const uint32_t *__restrict__ fnext,
@@ -835,7 +904,7 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
                                          float *mq, float *mpartial,
                                          const uint32_t *__restrict__ reach, uint32_t *ctr,
                                          uint32_t *su, uint32_t *sg, const uint32_t *lst,
-                                         uint32_t lcnt, uint32_t lheavy)
+                                         uint32_t lcnt, uint32_t lheavy, WC &wc)
 {
     const unsigned lane = lane_id();
     // heavy span items only when a heavy vertex is at this depth
@@ -849,14 +918,16 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
         if (t < nhi) {
             const uint32_t v = a.hitem_v[t];
             const uint32_t f = fd[v] & dmask;
+            if (lane == 0) wc.add(WC_BYTES, 4);  // level mask
             if (!f) continue;
             float P = 0.0f;
             if (!no_succ) {
                 const float sv = __uint2float_rn(((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u);
                 const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
-                P = dep_span(a, f, sv, b0, min(a.col[v + 1], b0 + AXBC_SPAN), fnext, mq, su, sg);
+                P = dep_span(a, f, sv, b0, min(a.col[v + 1], b0 + AXBC_SPAN), fnext, mq, su, sg, wc);
             }
             mpartial[(uint64_t)t * AXBC_W + lane] = P;
+            if ((f >> lane) & 1u) wc.add(WC_BYTES, 8);  // path count read, span partial written
             continue;
         }
         if (lst) {
@@ -865,8 +936,9 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
             if (lane < ent && i < lcnt) {
                 v_l = lst[i];
                 if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fd[v_l] & dmask;
+                wc.add(WC_BYTES, 8);  // list entry, level mask
             }
-            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg);
+            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg, wc);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
@@ -876,19 +948,23 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
             if (lane < cnt) {
                 v_l = a.order[beg + lane];
                 f_l = fd[v_l] & dmask;
+                wc.add(WC_BYTES, 4);  // level mask
             }
-            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg);
+            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg, wc);
         }
     }
 }
 
 // One backward depth, device-driven: d = bi->bd (a no-op once below 0).
+// CNT: the counting build (work counts into wc[KP_BWD]).
+template <bool CNT>
 __global__ void __launch_bounds__(BATCH_TPB, AXBC_BWD_MIN_BLOCKS) k_bwd_step(Adj a, const BatchInfo *__restrict__ bi,
                                                         uint32_t *const *__restrict__ tab,
                                                         const uint32_t *__restrict__ msigma,
                                                         float *mdelta, float *mq, float *mpartial,
                                                         const uint32_t *__restrict__ reach,
-                                                        uint32_t *ctrs, LevelLists ll)
+                                                        uint32_t *ctrs, LevelLists ll,
+                                                        unsigned long long *wc)
 {
     __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
     __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
@@ -899,8 +975,10 @@ __global__ void __launch_bounds__(BATCH_TPB, AXBC_BWD_MIN_BLOCKS) k_bwd_step(Adj
     uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
     uint32_t lcnt = 0;
     const uint32_t *lst = level_list(ll, d, lcnt);
+    WorkCount<CNT> cnt;
     bwd_body(a, dmask, d == bi->dmax, tab[d], tab[d + 1], msigma, mdelta, mq, mpartial, reach,
-             ctrs + 2 * d + 1, su, sg, lst, lcnt, ll.heavy[d]);
+             ctrs + 2 * d + 1, su, sg, lst, lcnt, ll.heavy[d], cnt);
+    cnt.flush(wc);
 }
 
 __device__ __forceinline__ void combine_body(const Adj &a, uint32_t dmask,
@@ -1280,9 +1358,9 @@ static int dyn_grid(axbc_ctx *c)
     // dynamic kernels: as many blocks as stay resident; work comes from counters
     if (!c->dyn_blocks_per_sm) {
         int a = 0, b = 0, d = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_step, BATCH_TPB, 0));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step, BATCH_TPB, 0));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_fwd_pull_step, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_step<false>, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step<false>, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_fwd_pull_step<false>, BATCH_TPB, 0));
         c->dyn_blocks_per_sm = std::max(1, a);
         c->pull_blocks_per_sm = std::max(1, d);
         c->bwd_blocks_per_sm = std::max(1, b);
@@ -1307,10 +1385,10 @@ static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
 {
     axbc_graph *g = c->g;
     const LevelLists ll = lists_of(c);
-    k_fwd_push_step<<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->seen, c->msigma,
-                                                        c->ctrs, ll);
-    k_fwd_pull_step<<<pull_grid(c), BATCH_TPB, 0, c->stream>>>(g->rev, c->bi, c->fmtab, c->seen, c->msigma,
-                                                        c->ctrs, ll);
+    k_fwd_push_step<false><<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->seen, c->msigma,
+                                                               c->ctrs, ll, nullptr);
+    k_fwd_pull_step<false><<<pull_grid(c), BATCH_TPB, 0, c->stream>>>(g->rev, c->bi, c->fmtab, c->seen,
+                                                                      c->msigma, c->ctrs, ll, nullptr);
     k_stats_step<<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->fwd.col,
                                                      g->rev.col, g->reach, ll);
     k_level_advance<<<1, 32, 0, c->stream>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode,
@@ -1320,9 +1398,9 @@ static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
 static void bwd_step_kernels(axbc_ctx *c)
 {
     axbc_graph *g = c->g;
-    k_bwd_step<<<bwd_grid(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
-                                                   c->mq, c->mpartial, g->reach, c->ctrs,
-                                                   lists_of(c));
+    k_bwd_step<false><<<bwd_grid(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma,
+                                                                c->mdelta, c->mq, c->mpartial, g->reach,
+                                                                c->ctrs, lists_of(c), nullptr);
     if (g->fwd.n_heavy)
         k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, c->stream>>>(
             g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach,
@@ -1359,7 +1437,9 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     cudaStream_t s = c->stream;
     const int sgrid = axbc_grid_for(c, BATCH_TPB, 8);
     const int dgrid = dyn_grid(c);
-    const bool prof = c->prof_on;
+    // per-launch mode: profiling events around each kernel, or the counting builds
+    const bool prof = c->prof_on || c->count_on;
+    unsigned long long *wc = c->count_on ? c->wcount : nullptr;
     TRY(ensure_level_tables(c));
     TRY(axbc_batch_levels_alloc(c, 10));
     if (!prof) TRY(capture_steps(c, dgrid, sgrid));
@@ -1428,19 +1508,27 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
                 const int L = launched + i + 1;
                 {
                     ProfScope ps(c, KP_FWD_PUSH, 0);
-                    c->prof.back().tag = L;
-                    k_fwd_push_step<<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->seen,
-                                                                c->msigma, c->ctrs, ll);
+                    if (c->prof_on) c->prof.back().tag = L;
+                    if (wc)
+                        k_fwd_push_step<true><<<dgrid, BATCH_TPB, 0, s>>>(
+                            g->fwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PUSH * WC_NFIELDS);
+                    else
+                        k_fwd_push_step<false><<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->seen,
+                                                                           c->msigma, c->ctrs, ll, nullptr);
                 }
                 {
                     ProfScope ps(c, KP_FWD_PULL, 0);
-                    c->prof.back().tag = L;
-                    k_fwd_pull_step<<<pull_grid(c), BATCH_TPB, 0, s>>>(g->rev, c->bi, c->fmtab, c->seen,
-                                                                c->msigma, c->ctrs, ll);
+                    if (c->prof_on) c->prof.back().tag = L;
+                    if (wc)
+                        k_fwd_pull_step<true><<<pull_grid(c), BATCH_TPB, 0, s>>>(
+                            g->rev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PULL * WC_NFIELDS);
+                    else
+                        k_fwd_pull_step<false><<<pull_grid(c), BATCH_TPB, 0, s>>>(
+                            g->rev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
                 }
                 {
                     ProfScope ps(c, KP_LEVEL_STATS, 0);
-                    c->prof.back().tag = L;
+                    if (c->prof_on) c->prof.back().tag = L;
                     k_stats_step<<<sgrid, BATCH_TPB, 0, s>>>(n, c->bi, c->fmtab, c->seen, g->fwd.col,
                                                              g->rev.col, g->reach, ll);
                 }
@@ -1468,7 +1556,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     // per-level totals for the byte model of the profiling hooks
     std::vector<unsigned long long> lte, lcnt;
     std::vector<int32_t> lmode;
-    if (prof) {
+    if (c->prof_on) {
         lte.resize(L + 1);
         lcnt.resize(L + 1);
         lmode.resize(L + 1);
@@ -1501,20 +1589,29 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
                 c->launches += g->fwd.n_heavy ? 3 : 2;
                 continue;
             }
-            if (d == Dmax) depth0 = c->bi_host->depth0mask;
+            if (d == Dmax && c->prof_on) depth0 = c->bi_host->depth0mask;
             const double W = nsrc;
-            double te_d = (double)lte[d], cnt_d = (double)lcnt[d];
-            if (d == 0) {
-                const double frac = (double)__builtin_popcount(depth0) / W;
-                te_d *= frac;
-                cnt_d *= frac;
+            double bytes = 0.0;
+            if (c->prof_on) {
+                double te_d = (double)lte[d], cnt_d = (double)lcnt[d];
+                if (d == 0) {
+                    const double frac = (double)__builtin_popcount(depth0) / W;
+                    te_d *= frac;
+                    cnt_d *= frac;
+                }
+                bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
             }
-            const double bytes = d == Dmax ? cnt_d * 4.0 : te_d * (4.0 / W + 8.0);
             {
                 ProfScope ps(c, KP_BWD, bytes);
-                if (prof) c->prof.back().tag = d;
-                k_bwd_step<<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta,
-                                                       c->mq, c->mpartial, g->reach, c->ctrs, ll);
+                if (c->prof_on) c->prof.back().tag = d;
+                if (wc)
+                    k_bwd_step<true><<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma,
+                                                                      c->mdelta, c->mq, c->mpartial, g->reach,
+                                                                      c->ctrs, ll, wc + KP_BWD * WC_NFIELDS);
+                else
+                    k_bwd_step<false><<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma,
+                                                                       c->mdelta, c->mq, c->mpartial, g->reach,
+                                                                       c->ctrs, ll, nullptr);
             }
             if (g->fwd.n_heavy) {
                 ProfScope ps(c, KP_BWD_COMBINE, 0);

@@ -254,6 +254,10 @@ struct axbc_ctx {
     uint64_t launches = 0;
     bool prof_on = false;
     std::vector<ProfRec> prof;
+    // work counting: the traversal kernels' counting builds run instead of the
+    // captured level steps, accumulating into wcount[kind][field]
+    bool count_on = false;
+    unsigned long long *wcount = nullptr;  // KP_NKINDS * WC_NFIELDS
     std::vector<cudaEvent_t> ev_pool;
     double level_te_prev = 0;  // degree sum of the previous level's new vertices
     std::vector<double> level_te;
@@ -334,6 +338,31 @@ struct ProfScope {
 
 // ---------------------------------------------------------------- device helpers
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Work counts of the traversal kernels, kept only in their counting builds
+// (axbc_ctx_count): per launch kind the bytes the launch has to move at least
+// (each 4-byte word it must read or write once, sectors not counted),
+// adjacency entries scanned, (edge, pivot) gathers and (vertex, pivot) results
+// written.  The plain builds carry an empty counter that compiles away.
+enum { WC_BYTES = 0, WC_ENTRIES, WC_GATHERS, WC_PAIRS, WC_NFIELDS };
+template <bool ON> struct WorkCount {
+    __device__ __forceinline__ void add(int, unsigned long long) {}
+    __device__ __forceinline__ void flush(unsigned long long *) {}
+};
+template <> struct WorkCount<true> {
+    unsigned long long f[WC_NFIELDS] = {0, 0, 0, 0};
+    __device__ __forceinline__ void add(int i, unsigned long long x) { f[i] += x; }
+    // every lane of the warp calls this once, at the end of the kernel
+    __device__ __forceinline__ void flush(unsigned long long *w)
+    {
+#pragma unroll
+        for (int i = 0; i < WC_NFIELDS; i++) {
+            unsigned long long x = f[i];
+            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane_id() == 0 && x) atomicAdd(&w[i], x);
+        }
+    }
+};
 
 // One successor's share of a dependency, in the reference's operation order
 // (scan_frt_mono: (delta[r] + 1) / sigma[r] * sigma[c]), rounded op by op.

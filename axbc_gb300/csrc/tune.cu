@@ -67,12 +67,41 @@ static int run_plain_trial(axbc_ctx *c, void *arg)
     return AXBC_OK;
 }
 
+static int tune_trials(axbc_ctx *c, const uint32_t *pivots, int npivots, int H, axbc_tuning *out);
+
 extern "C" int axbc_autotune(axbc_ctx *c, const uint32_t *pivots, int npivots, int H,
                              axbc_tuning *out)
 {
     CHECK_ARG(c && pivots && out, "axbc_autotune: null argument");
     CHECK_ARG(npivots >= 1, "axbc_autotune: need at least one trial pivot");
     for (int i = 0; i < npivots; i++) CHECK_ARG(pivots[i] < c->g->n, "axbc_autotune: pivot >= n");
+    // the trial passes add into bc: the context's bc and last dependency vector
+    // are set aside first and put back at the end, so tuning leaves its results
+    // as they were
+    const uint64_t n = c->g->n;
+    DBuf keep;
+    TRY(keep.alloc(2 * n * 4));
+    CU(cudaMemcpyAsync(keep.as<float>(), c->bc, n * 4, cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(keep.as<float>() + n, c->delta_last, n * 4, cudaMemcpyDeviceToDevice, c->stream));
+    const bool dl_valid = c->delta_last_valid;
+    const double f_batch0 = c->push_factor_batch, f_single0 = c->push_factor_single;
+    int rc = tune_trials(c, pivots, npivots, H, out);
+    if (rc != AXBC_OK) {
+        c->push_factor_batch = f_batch0;
+        c->push_factor_single = f_single0;
+    }
+    cudaError_t e = cudaMemcpyAsync(c->bc, keep.as<float>(), n * 4, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->delta_last, keep.as<float>() + n, n * 4, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    c->delta_last_valid = dl_valid;
+    if (rc == AXBC_OK && e != cudaSuccess) return axbc_cuda_fail(e, "autotune restore", __FILE__, __LINE__);
+    return rc;
+}
+
+// the timed trials of axbc_autotune; leaves the chosen factors in the context
+static int tune_trials(axbc_ctx *c, const uint32_t *pivots, int npivots, int H, axbc_tuning *out)
+{
     // all trial pivots (up to 4 batches), each candidate timed as the best of 2
     const int kb = std::min(npivots, 4 * AXBC_MAX_BATCH);
     std::vector<double> p(kb, 1.0 / (double)c->g->n);
@@ -119,7 +148,6 @@ extern "C" int axbc_autotune(axbc_ctx *c, const uint32_t *pivots, int npivots, i
         }
     }
     c->push_factor_single = best_fs;
-    TRY(axbc_ctx_reset(c));
     out->push_factor_single = best_fs;
     out->push_factor_batch = best_f;
     out->batch_width = best_w;

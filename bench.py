@@ -1,19 +1,24 @@
 #!/usr/bin/env python3
-"""Benchmark: BC traversed-edges/s (forward + backward) on GB300.
+"""Benchmark: BC traversed-edges/s (forward + backward) on GB300, and the
+serving configuration's p50/p99 request latency.
 
-Workload (the headline configuration): Kronecker/R-MAT scale 23, edgefactor 16,
-undirected, heuristic 3 (bc-based dynamic sampling), 1024 pivots per step in
-batches of 32, Bader test off.  One step is one sampled BC run of 1024 pivots:
-device sampling, the batched forward/backward passes and the bc updates.  TE
-per pivot = 2 * degree sum of the vertices it reaches (Graph500 counting).
+Workload (the headline configuration): the Graph500 generator's Kronecker graph
+at scale 23, edgefactor 16 (seeds 23/24), undirected, heuristic 3 (bc-based
+dynamic sampling), 1024 pivots per step in batches of 32, Bader test off.  One
+step is one sampled BC run of 1024 pivots: device sampling, the batched
+forward/backward passes and the bc updates.  TE per pivot = 2 * degree sum of
+the vertices it reaches (Graph500 counting).  After the headline timing a
+serving phase runs the request server under Poisson arrivals (resident graphs:
+Kronecker scales 16/18/20/22 and a 1024^2 grid) and reports p50/p99 latency.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 --impl reference times the oracle (oracle/, a C restatement of the reference
-path; the reference itself cannot be built here) on the host cores with
-OpenMP, on a bounded pivot sample of the same graph and pivot list.
+path; the reference needs MPI and a Kepler-era toolchain and is not run on the
+GPU machine) on the host cores with OpenMP, on a bounded pivot sample of the same
+graph and pivot list.
 
-Input generation (device R-MAT + CSC build) is set-up and is not timed.
+Input generation (device generator + CSC build) is set-up and is not timed.
 The graph (~1.1 GB of adjacency) is larger than L2, so no L2 flush is needed.
 """
 from __future__ import annotations
@@ -37,6 +42,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=23)
+    ap.add_argument("--graph", default="kron",
+                    help="headline graph: kron (Graph500 generator at --scale) or grid:SIDE "
+                         "(SIDE x SIDE grid, 2%% of edges dropped, 0.01%% long-range, seed 7)")
     ap.add_argument("--edgefactor", type=int, default=16)
     ap.add_argument("--pivots", type=int, default=1024, help="pivots per step")
     ap.add_argument("--width", type=int, default=32, help="batch width")
@@ -46,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no e2e pass")
     ap.add_argument("--skip-plain", action="store_true", help="profiling runs: no plain pass")
+    ap.add_argument("--skip-serving", action="store_true", help="no serving phase after the headline")
+    ap.add_argument("--skip-count", action="store_true", help="no counted step (roofline bytes)")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "serving", "config1", "config2", "config3"],
                     help="serving: the request server on resident graphs (p50/p99 latency); "
@@ -117,17 +127,31 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def kernel_source_digest():
+    """SHA-256 of the traversal kernels' source file: a DRAM figure taken from an
+    ncu capture of other kernel code is stale."""
+    import hashlib
+    with open(os.path.join(ROOT, "axbc_gb300", "csrc", "batch.cu"), "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
 def traffic_for(kernel, graph_key):
-    """Per-launch DRAM bytes of `kernel` on this graph from the committed ncu summary
-    (profiles/traffic.json, written from profiles/dram_traffic_*.md), if any."""
+    """(per-launch DRAM bytes of `kernel` on this graph from the committed ncu
+    capture in profiles/traffic.json, note).  None when there is no capture for
+    this graph and kernel, or when it was taken of other kernel source."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
-        ent = t.get(graph_key, {}).get(kernel)
-        return None if ent is None else float(ent["dram_bytes_per_launch"])
     except Exception:
-        return None
+        return None, "no ncu capture committed"
+    ent = t.get(graph_key, {})
+    k = ent.get("kernels", {}).get(kernel)
+    if k is None:
+        return None, f"no ncu capture of {kernel} on {graph_key}"
+    if ent.get("kernel_source_sha256") != kernel_source_digest():
+        return None, "the committed ncu capture is of other kernel source (stale)"
+    return float(k["dram_bytes_per_launch"]), f"ncu capture at {ent.get('commit', '?')}"
 
 
 class _DeviceArray:
@@ -265,7 +289,7 @@ def config_bench(args):
     print(json.dumps(out), flush=True)
 
 
-def serve_bench(args):
+def serve_bench(args, emit=True):
     """The request server under Poisson arrivals (seed 11) over resident graphs:
     Kronecker scales 16, 18, 20, 22 (edgefactor 16) and a 1024x1024 grid.  Each
     request picks a graph and a heuristic -z 0..5 uniformly, width 8, and either
@@ -334,8 +358,12 @@ def serve_bench(args):
            "clocks": clk}
     if failed:
         out["errors"] = failed[:3]
-    print(json.dumps(out), flush=True)
     srv.close()
+    for _, G in graphs:
+        G.close()
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def main():
@@ -368,9 +396,16 @@ def main():
     # the reference's own input: the Graph500 generator with gen_graph's seeds
     # (23, 24) and initiator, generated and built on the device (set-up, untimed)
     t_graph = time.perf_counter()
-    G = ax.Graph.kronecker(args.scale, args.edgefactor, 23, 24)
-    config["graph"] = {"generator": "Graph500 (seeds 23/24, initiator .57/.19/.19/.05)",
-                       "n": G.n, "m": G.m, "build_s": round(time.perf_counter() - t_graph, 3)}
+    if args.graph == "kron":
+        G = ax.Graph.kronecker(args.scale, args.edgefactor, 23, 24)
+        gen = "Graph500 (seeds 23/24, initiator .57/.19/.19/.05)"
+    else:
+        side = int(args.graph.split(":")[1])
+        G = ax.Graph.grid(side, 0.02, 1e-4, seed=7)
+        gen = f"{side}x{side} grid, 2% of edges dropped, 0.01% long-range edges, seed 7"
+        config["workload"] = workload.replace(f"kronecker-s{args.scale}-ef{args.edgefactor}", f"grid-{side}")
+    config["graph"] = {"generator": gen, "n": G.n, "m": G.m,
+                       "build_s": round(time.perf_counter() - t_graph, 3)}
     stream = torch.cuda.Stream()
     ctx = ax.Context(G, stream=stream.cuda_stream)
 
@@ -468,59 +503,86 @@ def main():
     te_all = sharding.total(float(te), device="cuda")
     value = te_all / t
 
-    # roofline of the dominant kernel kind
+    # ---- roofline of the dominant kernel kind (largest live CUDA-event time)
     peak, peak_kind = peaks()
     kind = max(prof, key=lambda k: prof[k][0])
-    ms, cnt, by = prof[kind]
-    achieved = (by / (ms / 1000.0)) / 1e9 if ms > 0 else 0.0
-    kernel = ax.PROF_KERNELS[kind]
-    traffic = traffic_for(kernel, f"kronecker-s{args.scale}-ef{args.edgefactor}")
+    ms, cnt, model_by = prof[kind]
     avg_s = ms / max(cnt, 1) / 1000.0
+    kernel = ax.PROF_KERNELS[kind]
+    graph_key = (f"kronecker-s{args.scale}-ef{args.edgefactor}" if args.graph == "kron"
+                 else f"grid-{args.graph.split(':')[1]}")
+    # the bytes it must move: one more step through the counting builds of the
+    # traversal kernels (every step draws the same pivots: same seed, bc reset)
+    counts = {}
+    if not args.skip_count:
+        ctx.count(True)
+        step(seed)
+        counts = ctx.count_read()
+        ctx.count(False)
+    must = counts.get(kind, {}).get("bytes")
+    must_per_launch = must * args.steps / max(cnt, 1) if must else None
+    traffic, traffic_note = traffic_for(kernel, graph_key)
+    if must_per_launch:
+        achieved = must_per_launch / avg_s / 1e9
+        basis = ("bytes the kernel must move, counted on the device by its counting build over "
+                 "one step: each 4-byte word read or written once (adjacency entries, level "
+                 "masks, neighbours' per-pivot values, results); 32-byte sectors not counted")
+    else:
+        achieved = (model_by / (ms / 1000.0)) / 1e9 if ms > 0 else 0.0
+        basis = "traversed-edge byte model (no counting build for this kernel kind)"
+    model_gbs = (model_by / (ms / 1000.0)) / 1e9 if ms > 0 else 0.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-                "model": "traversed-edge bytes, Graph500 counting: (4/W+8) B/TE backward, (4/W+4) "
-                         "forward; counts every edge of a reached vertex",
-                "dram_gbs_from_traffic": (traffic / avg_s / 1e9) if traffic else None,
-                "dram_frac_from_traffic": (traffic / avg_s / 1e9 / peak) if traffic else None,
+                "achieved_basis": basis,
+                "must_move_bytes_per_launch": must_per_launch,
+                "work_per_step": counts.get(kind),
+                "dram_gbs": (traffic / avg_s / 1e9) if traffic else None,
+                "dram_frac": (traffic / avg_s / 1e9 / peak) if traffic else None,
+                "traffic_source": traffic_note,
+                "model": "traversed-edge byte model, Graph500 counting: (4/W+8) B/TE backward, "
+                         "(4/W+4) forward, charged to every edge of a reached vertex (over-counts: "
+                         "the backward gathers only successors)",
+                "model_bytes_per_launch": model_by / max(cnt, 1),
+                "model_frac": model_gbs / peak,
                 "launches": cnt, "avg_launch_ms": ms / max(cnt, 1),
-                "algorithmic_bytes_per_launch": by / max(cnt, 1),
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "share_of_kernel_time": ms / max(sum(v[0] for v in prof.values()), 1e-9),
-                "kernel_ms": {k: round(v[0], 3) for k, v in prof.items() if v[1]}}
+                "kernel_ms": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
+                "must_move_bytes_per_step": {k: v["bytes"] for k, v in counts.items()}}
 
-    # e2e: the same pivots through the host-buffer C ABI (pinned inputs/outputs)
+    # ---- e2e: the plugin call a user makes for this workload, host side:
+    # axbc_run_sampled with the request in host memory, then the pivot list and
+    # bc read back into host memory (pinned), every step
     piv = last["pivots"]
     pr = last["probs"]
-    nb = (len(piv) + args.width - 1) // args.width
-    h_piv = torch.from_numpy(piv.astype(np.uint32).view(np.int32)).pin_memory()
-    h_pr = torch.from_numpy(pr.astype(np.float64)).pin_memory()
+    import ctypes
     h_bc = torch.empty(G.n, dtype=torch.float32).pin_memory()
-    piv_np, pr_np, bc_np = h_piv.numpy().view(np.uint32), h_pr.numpy(), h_bc.numpy()
+    bc_ptr = ctypes.c_void_p(h_bc.data_ptr())
 
     def e2e_step_():
-        ctx.reset()
-        tot = 0
-        for b in range(nb):
-            sl = slice(b * args.width, min(len(piv), (b + 1) * args.width))
-            st = ctx.run_batch(piv_np[sl], pr_np[sl], 0)
-            tot += sum(s["te"] for s in st)
-        import ctypes
-        ax._check(ax.lib().axbc_get_bc(ctx._h, bc_np.ctypes.data_as(ctypes.c_void_p)))
-        return tot
+        r = step(seed)  # run_sampled + axbc_get_pivots (host vectors)
+        ax._check(ax.lib().axbc_get_bc(ctx._h, bc_ptr))
+        return r["te"], len(r["pivots"])
 
     e2e = None
     if not args.skip_e2e:
+        ctx.profile(False)
         e2e_step_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e2e_te = 0
+        k_piv = 0
         for _ in range(args.steps):
-            e2e_te += e2e_step_()
+            te_i, k_piv = e2e_step_()
+            e2e_te += te_i
         torch.cuda.synchronize()
         e2e_t = time.perf_counter() - t0
         e2e = {"value": e2e_te * world / e2e_t, "unit": "TE/s",
-               "h2d_bytes_per_step": int(len(piv) * 12), "d2h_bytes_per_step": int(G.n * 4),
-               "api": "axbc_run_batch (host pivot/p arrays) + axbc_get_bc (pinned host bc)"}
+               "h2d_bytes_per_step": int(ctypes.sizeof(ax.RunParams)),
+               "d2h_bytes_per_step": int(G.n * 4 + k_piv * 12),
+               "api": "axbc_run_sampled (request parameters from host memory; device sampler, "
+                      "batched passes, bc updates) + axbc_get_pivots + axbc_get_bc into pinned "
+                      "host memory; wall clock, profiling off"}
 
     # the plain form (one pivot per launch sequence, host-driven levels) on a
     # sample of the same pivots: the denominator of the batched form's speed-up
@@ -559,6 +621,17 @@ def main():
                                          "OpenMP over pivots (oracle/ C restatement)",
                                "single_thread": {"value": v1, "unit": "TE/s", "cores": 1,
                                                  "sample": f"the first pivot of the list in {dt1:.1f} s"}}
+    if rank == 0 and world == 1 and not args.skip_serving:
+        # the serving configuration after the headline: resident graphs,
+        # Poisson arrivals, continuous batching; p50/p99 request latency
+        ctx.close()
+        G.close()
+        torch.cuda.synchronize()
+        srv = serve_bench(args, emit=False)
+        out["serving"] = {k: srv[k] for k in ("p50_s", "p99_s", "mean_queue_wait_s", "requests",
+                                             "failed", "throughput_te_per_s", "requests_per_s",
+                                             "span_s", "passes", "lanes_per_pass", "p50_by_graph_s",
+                                             "config", "clocks") if k in srv}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

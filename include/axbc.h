@@ -147,7 +147,9 @@ int axbc_ctx_set_tuning(axbc_ctx *ctx, double push_factor_single, double push_fa
 /* Autotuner: times trial passes from the given pivots (up to 128 batched, in
  * batches of the width; the first 4 plain) over a grid of direction-switch
  * factors and batch widths, keeps the fastest setting in the context and
- * returns it.  bc is reset to zero afterwards. */
+ * returns it.  The context's bc and last dependency vector come back as they
+ * were before the call: both are copied aside first and restored after the
+ * trial passes.  On failure the factors stay unchanged. */
 typedef struct {
     double push_factor_single;
     double push_factor_batch;
@@ -347,6 +349,19 @@ int axbc_ctx_profile_records(axbc_ctx *ctx, int32_t *kinds, int32_t *tags, float
                              uint64_t cap, uint64_t *count);
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
+
+/* ---- work counting ----
+ * With counting on, batched passes launch counting builds of the forward
+ * push, forward pull and backward kernels (one launch per level, as with
+ * profiling; slower, for measurement only).  Per kind (AXBC_PROF_KINDS order)
+ * four counters: the bytes the launches must move at least (every 4-byte word
+ * they must read or write once, whole sectors not counted), adjacency entries
+ * scanned, (edge, pivot) gathers of a neighbour's per-pivot value, and
+ * (vertex, pivot) values written.  No counterpart in the reference. */
+#define AXBC_WORK_FIELDS 4
+int axbc_ctx_count(axbc_ctx *ctx, int enable);
+/* counts[kind * AXBC_WORK_FIELDS + field] for kinds < nkinds since the last read; clears them */
+int axbc_ctx_count_read(axbc_ctx *ctx, uint64_t *counts, int nkinds);
 
 /* Test hooks: the next n device allocations made by the library fail with
  * AXBC_ERR_NOMEM (host-side failure injection; 0 clears it); or the

@@ -64,14 +64,24 @@ class RunResult(C.Structure):
     ]
 
 
+def reference_dir():
+    """The reference's source tree, when present on this machine: the
+    AXBC_REFERENCE_DIR environment variable, else a `reference` directory
+    beside the repository.  None where it does not exist (the GPU machine)."""
+    d = os.environ.get("AXBC_REFERENCE_DIR") or os.path.join(_HERE, "..", "..", "reference")
+    d = os.path.abspath(d)
+    return d if os.path.isdir(os.path.join(d, "generator")) else None
+
+
 def build(force: bool = False, ref: bool = False) -> None:
     """Compile liboracle.so (and the reference generator shim if asked)."""
     target = os.path.join(_HERE, "liboracle.so")
     newest = max(os.path.getmtime(os.path.join(_HERE, f)) for f in ("oracle.c", "oracle.h", "kron.c"))
     if force or not os.path.exists(target) or os.path.getmtime(target) < newest:
         subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
-    if ref and os.path.isdir("/root/reference/generator"):
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    rd = reference_dir() if ref else None
+    if rd:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={rd}"], check=True)
 
 
 def lib():
