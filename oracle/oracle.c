@@ -284,9 +284,11 @@ static float dependency(const orc_graph *g, uint32_t c, int d, const int32_t *lv
  * bc_func_mono (src/axbc2d.c:1514-1659) + scan_col_mono2 (:588-658) +
  * scan_frt_mono (:719-772) + pre_update_bc_cuda (:358-373, gated by -H 1 at
  * src/axbc2d.c:1636) + update_bc (:269-286). */
-static int bc_pivot_ws(const orc_graph *g, uint32_t v0, double p, int H, int order, float *bc,
-                       int32_t *lvl, uint32_t *sigma, float *delta, uint32_t *queue,
-                       uint64_t *levstart, orc_pivot_stats *st)
+/* The traversal of one pivot: levels, path counts, dependencies and the
+ * counts its bc update needs (st->all includes reach[v0]). */
+static int pivot_traverse(const orc_graph *g, uint32_t v0, int H, int order, int32_t *lvl,
+                          uint32_t *sigma, float *delta, uint32_t *queue, uint64_t *levstart,
+                          orc_pivot_stats *st)
 {
     const uint64_t n = g->n;
     uint64_t v, q, qend, nvisited = 1, te = 0;
@@ -353,23 +355,39 @@ static int bc_pivot_ws(const orc_graph *g, uint32_t v0, double p, int H, int ord
         uint32_t c = queue[q];
         te += (uint64_t)(g->col[c + 1] - g->col[c]);
     }
+    st->nvisited = nvisited;
+    st->all = all;
+    st->te = 2 * te;
+    st->levels = level;
+    return 0;
+}
 
-    {
-        const uint64_t nv = nvisited + all;
-        for (v = 0; v < n; v++) {
-            if (v == v0) {
-                if (reach_v0 > 0) bc[v] = bc[v] + (float)((uint64_t)reach_v0 * (nv - 2));
-                continue;
-            }
-            bc[v] = bc[v] + (float)((double)(delta[v] * (float)(reach_v0 + 1u)) / p);
+/* update_bc (src/cuda_kernels.cu:269-286) with the traversal's dependencies */
+static void pivot_apply(const orc_graph *g, uint32_t v0, double p, const float *delta,
+                        const orc_pivot_stats *st, float *bc)
+{
+    const uint64_t n = g->n, nv = st->nvisited + st->all;
+    const uint32_t reach_v0 = g->reach[v0];
+    uint64_t v;
+    for (v = 0; v < n; v++) {
+        if (v == v0) {
+            if (reach_v0 > 0) bc[v] = bc[v] + (float)((uint64_t)reach_v0 * (nv - 2));
+            continue;
         }
+        bc[v] = bc[v] + (float)((double)(delta[v] * (float)(reach_v0 + 1u)) / p);
     }
-    if (st) {
-        st->nvisited = nvisited;
-        st->all = all;
-        st->te = 2 * te;
-        st->levels = level;
-    }
+}
+
+static int bc_pivot_ws(const orc_graph *g, uint32_t v0, double p, int H, int order, float *bc,
+                       int32_t *lvl, uint32_t *sigma, float *delta, uint32_t *queue,
+                       uint64_t *levstart, orc_pivot_stats *st)
+{
+    orc_pivot_stats s;
+    memset(&s, 0, sizeof(s));
+    int rc = pivot_traverse(g, v0, H, order, lvl, sigma, delta, queue, levstart, &s);
+    if (st) *st = s;
+    if (rc) return rc;
+    pivot_apply(g, v0, p, delta, &s, bc);
     return 0;
 }
 
@@ -685,11 +703,17 @@ int orc_run(const orc_graph *g, const orc_run_params *prm, float *bc_out, float 
     uint32_t *bv = (uint32_t *)malloc(W * sizeof(uint32_t));
     double *bp = (double *)malloc(W * sizeof(double));
     uint64_t *bskip = (uint64_t *)malloc(W * sizeof(uint64_t));
-    int32_t *lvl = (int32_t *)malloc((N + 1) * sizeof(int32_t));
-    uint32_t *sigma = (uint32_t *)malloc((N + 1) * sizeof(uint32_t));
-    float *delta = (float *)malloc((N + 1) * sizeof(float));
-    uint32_t *queue = (uint32_t *)malloc((N + 1) * sizeof(uint32_t));
-    uint64_t *levstart = (uint64_t *)malloc((N + 3) * sizeof(uint64_t));
+    /* per-thread traversal workspaces: a batch's pivots are traversed in
+     * parallel and applied in order, which gives the sequential result */
+#ifdef _OPENMP
+    const int nthr = (W > 1 && N >= 65536) ? omp_get_max_threads() : 1;
+#else
+    const int nthr = 1;
+#endif
+    int32_t **lvl = (int32_t **)calloc(nthr, sizeof(int32_t *));
+    uint32_t **sigma = (uint32_t **)calloc(nthr, sizeof(uint32_t *));
+    uint32_t **queue = (uint32_t **)calloc(nthr, sizeof(uint32_t *));
+    uint64_t **levstart = (uint64_t **)calloc(nthr, sizeof(uint64_t *));
     float **bdelta = (float **)calloc(W, sizeof(float *));
     orc_pivot_stats *bst = (orc_pivot_stats *)calloc(W, sizeof(orc_pivot_stats));
 
@@ -697,6 +721,12 @@ int orc_run(const orc_graph *g, const orc_run_params *prm, float *bc_out, float 
     memset(&sd, 0, sizeof(sd));
     memset(bc, 0, N * sizeof(float));
     for (i = 0; i < (uint64_t)W; i++) bdelta[i] = (float *)malloc((N + 1) * sizeof(float));
+    for (i = 0; i < (uint64_t)nthr; i++) {
+        lvl[i] = (int32_t *)malloc((N + 1) * sizeof(int32_t));
+        sigma[i] = (uint32_t *)malloc((N + 1) * sizeof(uint32_t));
+        queue[i] = (uint32_t *)malloc((N + 1) * sizeof(uint32_t));
+        levstart[i] = (uint64_t *)malloc((N + 3) * sizeof(uint64_t));
+    }
 
     /* int LIMxSAMPLE = N*N (src/axbc2d.c:2835): the product is truncated */
     LIM = (int)(uint32_t)(N * N);
@@ -858,7 +888,20 @@ int orc_run(const orc_graph *g, const orc_run_params *prm, float *bc_out, float 
             ui++;
         }
 
-        /* run the batch: each pivot against its own copy of the state */
+        /* run the batch: the pivots' traversals (in parallel when the graph
+         * is large), then their bc updates in order */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthr) if (nthr > 1 && nb > 1)
+#endif
+        for (j = 0; j < nb; j++) {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            pivot_traverse(g, bv[j], prm->H, prm->order, lvl[t], sigma[t], bdelta[j], queue[t],
+                           levstart[t], &bst[j]);
+        }
         for (j = 0; j < nb; j++) {
             /* Bader replay before pivot j > 0 of the batch */
             if (j > 0 && prm->bader_c > 0) {
@@ -868,8 +911,7 @@ int orc_run(const orc_graph *g, const orc_run_params *prm, float *bc_out, float 
                     break;
                 }
             }
-            bc_pivot_ws(g, bv[j], bp[j], prm->H, prm->order, bc, lvl, sigma, bdelta[j], queue,
-                        levstart, &bst[j]);
+            pivot_apply(g, bv[j], bp[j], bdelta[j], &bst[j], bc);
             res->skipped += bskip[j];
             if (pivots_out && res->nrounds < pivots_cap) {
                 pivots_out[res->nrounds] = bv[j];
@@ -915,9 +957,14 @@ int orc_run(const orc_graph *g, const orc_run_params *prm, float *bc_out, float 
     free(bv);
     free(bp);
     free(bskip);
+    for (i = 0; i < (uint64_t)nthr; i++) {
+        free(lvl[i]);
+        free(sigma[i]);
+        free(queue[i]);
+        free(levstart[i]);
+    }
     free(lvl);
     free(sigma);
-    free(delta);
     free(queue);
     free(levstart);
     free(sd.deg);
