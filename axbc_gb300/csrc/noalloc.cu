@@ -16,11 +16,14 @@
 // from the frontier, so no transpose is needed and directed graphs work.
 //
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (once per device, with that device current); make that
+// cudaGetSymbolAddress (once per device, with that device current, and again
+// only if the device's context changed, e.g. after cudaDeviceReset); make that
 // first call before any stream capture.  All calls share the array and it
 // keeps the last call's contents: every call clears what must start at zero.
 // Calls that overlap on the GPU (two host threads, or two streams) race on the
 // array: serialise them.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -121,7 +124,41 @@ __global__ void k_static_heavy(const uint32_t *__restrict__ col, uint32_t n, uin
 
 static std::mutex g_static_mu;
 static uint32_t *g_static_addr[AXBC_STATIC_MAX_DEVICES];
+// the context each cached address belongs to (driver context id, never
+// reused): after cudaDeviceReset, or when the caller makes another context
+// current, the array lives at another address and is looked up again
+static unsigned long long g_static_ctx[AXBC_STATIC_MAX_DEVICES];
 static uint64_t g_static_levstart[AXBC_STATIC_MAX_N + 2];
+
+// id of the context current on this thread (0: none yet), through the
+// driver's entry points as the runtime hands them out (no link to libcuda)
+static int current_ctx_id(unsigned long long *id)
+{
+    typedef CUresult (*get_current_t)(CUcontext *);
+    typedef CUresult (*get_id_t)(CUcontext, unsigned long long *);
+    static get_current_t get_current = nullptr;
+    static get_id_t get_id = nullptr;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        CU(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+        CU(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+            axbc_set_error("axbc_bc_pivot_static: the driver offers no cuCtxGetCurrent/cuCtxGetId");
+            return AXBC_ERR_CUDA;
+        }
+        get_current = (get_current_t)f1;
+        get_id = (get_id_t)f2;
+    }
+    CUcontext ctx = nullptr;
+    *id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return AXBC_OK;
+    if (get_id(ctx, id) != CUDA_SUCCESS) {
+        axbc_set_error("axbc_bc_pivot_static: cuCtxGetId failed");
+        return AXBC_ERR_CUDA;
+    }
+    return AXBC_OK;
+}
 
 static int static_scratch(uint32_t **out)
 {
@@ -131,12 +168,17 @@ static int static_scratch(uint32_t **out)
         axbc_set_error("device ordinal %d beyond %d", dev, AXBC_STATIC_MAX_DEVICES);
         return AXBC_ERR_RANGE;
     }
-    if (!g_static_addr[dev]) {
+    unsigned long long ctx = 0;
+    TRY(current_ctx_id(&ctx));
+    if (!g_static_addr[dev] || ctx == 0 || ctx != g_static_ctx[dev]) {
         void *p = nullptr;
         // the array's name is a host-side stand-in; the kernels need its
-        // device address, looked up once per device with the device current
+        // device address, looked up once per device (and context) with the
+        // device current
         CU(cudaGetSymbolAddress(&p, g_static_scratch));
         g_static_addr[dev] = (uint32_t *)p;
+        if (ctx == 0) TRY(current_ctx_id(&ctx));  // the lookup made the context current
+        g_static_ctx[dev] = ctx;
     }
     *out = g_static_addr[dev];
     return AXBC_OK;

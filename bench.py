@@ -548,7 +548,7 @@ def main():
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "share_of_kernel_time": ms / max(sum(v[0] for v in prof.values()), 1e-9),
                 "kernel_ms": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
-                "must_move_bytes_per_step": {k: v["bytes"] for k, v in counts.items()}}
+                "work_per_step_by_kind": counts}
 
     # ---- e2e: the plugin call a user makes for this workload, host side:
     # axbc_run_sampled with the request in host memory, then the pivot list and

@@ -189,8 +189,9 @@ int axbc_run_pivot(axbc_ctx *ctx, uint32_t v0, double p, int H, axbc_pivot_stats
  * loading the library holds until exit; graphs above 2^18 vertices, or with
  * more than 2^14 span items of vertices of degree > 1024, return
  * AXBC_ERR_RANGE.  The first call on a device looks the array's address up
- * (make it before any stream capture).  Calls share the array: overlapping
- * calls race, so serialise them.  Results equal axbc_run_pivot's. */
+ * (make it before any stream capture), and looks it up again when the
+ * device's context changed (after cudaDeviceReset).  Calls share the array:
+ * overlapping calls race, so serialise them.  Results equal axbc_run_pivot's. */
 int axbc_bc_pivot_static(const uint32_t *col, const uint32_t *row, const uint32_t *reach,
                          uint64_t n, uint64_t m, uint32_t v0, double p, int H, float *bc,
                          void *stream, axbc_pivot_stats *stats);
