@@ -116,6 +116,9 @@ _SIGS = {
     "axbc_ctx_profile_read": (C.c_int, [_P, _P, _P, _P, C.c_int]),
     "axbc_ctx_launches": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "axbc_ctx_count": (C.c_int, [_P, C.c_int]),
+    "axbc_ctx_set_persistent": (C.c_int, [_P, C.c_int, C.c_int]),
+    "axbc_selftest_grid_barrier": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.POINTER(C.c_int),
+                                             C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     "axbc_ctx_count_read": (C.c_int, [_P, _P, C.c_int]),
     "axbc_autotune": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(Tuning)]),
     "axbc_bc_pivot_static": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_uint64, C.c_uint32,
@@ -147,7 +150,7 @@ _SIGS = {
 
 PROF_KINDS = ["batch_fwd_push", "batch_fwd_pull", "batch_level_stats", "batch_bwd",
               "batch_bwd_combine", "batch_update", "sampler", "plain_fwd", "plain_bwd",
-              "plain_other"]
+              "plain_other", "batch_persistent"]
 # work counters per kind (axbc_ctx_count_read)
 WORK_FIELDS = ["bytes", "entries", "gathers", "pairs"]
 # kernel names behind each profiling kind (for matching ncu launch lists)
@@ -155,7 +158,7 @@ PROF_KERNELS = {"batch_fwd_push": "k_fwd_push_step", "batch_fwd_pull": "k_fwd_pu
                 "batch_level_stats": "k_stats_step", "batch_bwd": "k_bwd_step",
                 "batch_bwd_combine": "k_bwd_combine_step", "batch_update": "k_update_m",
                 "sampler": "k_sampler", "plain_fwd": "k_fwd_push1", "plain_bwd": "k_bwd1",
-                "plain_other": "k_update1"}
+                "plain_other": "k_update1", "batch_persistent": "k_traverse_persist"}
 
 
 def lib():
@@ -473,6 +476,10 @@ class Context:
         _check(lib().axbc_ctx_profile_read(self._h, _ptr(ms), _ptr(cnt), _ptr(by), k))
         return {PROF_KINDS[i]: (float(ms[i]), int(cnt[i]), float(by[i])) for i in range(k)}
 
+    def set_persistent(self, mode=0, blocks_per_sm=0):
+        """Batched passes as one persistent launch: 1 always, -1 never, 0 auto."""
+        _check(lib().axbc_ctx_set_persistent(self._h, int(mode), int(blocks_per_sm)))
+
     def count(self, enable=True):
         """Run the counting builds of the traversal kernels (measurement only)."""
         _check(lib().axbc_ctx_count(self._h, int(enable)))
@@ -588,6 +595,14 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def selftest_grid_barrier(blocks_per_sm=2, rounds=1000, budget_cycles=1 << 33, absent_block=-1):
+    """(failed barrier site or 0, barriers completed, ms) of the persistent loop's grid barrier."""
+    site, leads, ms = C.c_int(), C.c_uint32(), C.c_float()
+    _check(lib().axbc_selftest_grid_barrier(blocks_per_sm, rounds, budget_cycles, absent_block,
+                                            C.byref(site), C.byref(leads), C.byref(ms)))
+    return site.value, leads.value, ms.value
 
 
 def selftest_division(n=1 << 26, seed=1):

@@ -213,6 +213,7 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     axbc_dfree(c->bc);
     axbc_dfree(c->delta_last);
     axbc_dfree(c->wcount);
+    axbc_dfree(c->gsync);
     axbc_dfree(c->lvl);
     axbc_dfree(c->sigma);
     axbc_dfree(c->delta);

@@ -639,18 +639,12 @@ __device__ __forceinline__ void stats_vertex(uint64_t u, uint32_t srcmask,
     if ((sn & srcmask) != srcmask && (sn2 & srcmask) == srcmask) udec += rcol[u + 1] - rcol[u];
 }
 
-__global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo *bi,
-                                                          uint32_t *const *__restrict__ tab,
-                                                          uint32_t *seen,
-                                                          const uint32_t *__restrict__ col,
-                                                          const uint32_t *__restrict__ rcol,
-                                                          const uint32_t *__restrict__ reach,
-                                                          LevelLists ll)
+__device__ __forceinline__ void stats_body(uint64_t n, BatchInfo *bi, int L, uint32_t srcmask,
+                                           const uint32_t *__restrict__ fcur, uint32_t *seen,
+                                           const uint32_t *__restrict__ col,
+                                           const uint32_t *__restrict__ rcol,
+                                           const uint32_t *__restrict__ reach, const LevelLists &ll)
 {
-    if (!bi->alive) return;
-    const int L = bi->cur + 1;
-    const uint32_t srcmask = bi->srcmask;
-    const uint32_t *__restrict__ fcur = tab[L];
     const unsigned lane = lane_id();
     const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
@@ -712,15 +706,29 @@ __global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo 
     }
 }
 
+__global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo *bi,
+                                                          uint32_t *const *__restrict__ tab,
+                                                          uint32_t *seen,
+                                                          const uint32_t *__restrict__ col,
+                                                          const uint32_t *__restrict__ rcol,
+                                                          const uint32_t *__restrict__ reach,
+                                                          LevelLists ll)
+{
+    if (!bi->alive) return;
+    const int L = bi->cur + 1;
+    stats_body(n, bi, L, bi->srcmask, tab[L], seen, col, rcol, reach, ll);
+}
+
 // Close forward level L = bi->cur + 1: per-pivot termination, the per-level
 // totals, the direction of the next level, and -- once nothing was discovered
 // -- the deepest depth and the depth-0 pivots of the backward pass.
-__global__ void k_level_advance(BatchInfo *bi, unsigned long long *level_te,
-                                unsigned long long *level_cnt, int32_t *level_mode,
-                                LevelLists ll, uint32_t pool_cap, uint32_t list_max)
+// one warp (lanes = pivots) of the block that closes level L
+__device__ __forceinline__ void level_advance_warp(BatchInfo *bi, unsigned long long *level_te,
+                                                   unsigned long long *level_cnt, int32_t *level_mode,
+                                                   const LevelLists &ll, uint32_t pool_cap,
+                                                   uint32_t list_max)
 {
-    const unsigned s = threadIdx.x;
-    if (!bi->alive) return;
+    const unsigned s = lane_id();
     const int L = bi->cur + 1;
     const uint32_t nsrc = bi->nsrc;
     const unsigned long long nw = s < nsrc ? bi->lvl_new[s] : 0ull;
@@ -759,6 +767,14 @@ __global__ void k_level_advance(BatchInfo *bi, unsigned long long *level_te,
         bi->any_new = 0;
     }
     if (s < AXBC_W) bi->lvl_new[s] = 0;
+}
+
+__global__ void k_level_advance(BatchInfo *bi, unsigned long long *level_te,
+                                unsigned long long *level_cnt, int32_t *level_mode,
+                                LevelLists ll, uint32_t pool_cap, uint32_t list_max)
+{
+    if (!bi->alive) return;
+    level_advance_warp(bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max);
 }
 
 // Sum of the 8 staged successor terms of one group as a balanced tree (pairs
@@ -1019,6 +1035,166 @@ __global__ void k_bwd_combine_step(Adj a, const BatchInfo *__restrict__ bi,
 __global__ void k_bwd_advance(BatchInfo *bi)
 {
     if (bi->bd >= 0) bi->bd--;
+}
+
+// ------------------------------------------------ persistent level loop
+// On graphs of many narrow levels (grids, roads) a level's work is a few
+// microseconds and the four launches per forward level and three per
+// backward depth dominate.  k_traverse_persist runs a whole batch -- every
+// forward level, then every backward depth -- in one cooperative launch whose
+// blocks are all resident, with the step kernels' device bodies separated by a
+// grid barrier: two barriers per forward level (expansion | statistics and
+// level close) and one or two per backward depth.
+
+// Wait budget of one barrier in SM clock cycles (about 4 s at 2 GHz): a wait
+// that runs out records its site and every block returns; the host reports
+// AXBC_ERR_TIMEOUT.
+#define AXBC_BAR_BUDGET (1ll << 33)
+
+__device__ __forceinline__ unsigned vload_u(const unsigned *p) { return *(const volatile unsigned *)p; }
+__device__ __forceinline__ int vload_i(const int *p) { return *(const volatile int *)p; }
+
+// All blocks of the cooperative grid meet here.  The last block to arrive runs
+// lead() with its first warp, then releases the others.  Thread 0 of each block
+// fences before arriving and after the wait, as cooperative groups' grid sync
+// does, so the block's later loads see what every block wrote before
+// arriving.  Returns false when this wait, or an earlier one of any block, ran
+// out of its budget.
+struct NoLead {
+    __device__ void operator()() const {}
+};
+template <class F>
+__device__ __forceinline__ bool grid_barrier(GridSync *gs, long long budget, int site, const F &lead)
+{
+    __shared__ int s_role;  // 1 leader, 0 released, -1 failed
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned g = vload_u(&gs->gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(&gs->count, 1u);
+        int role = arrived == gridDim.x - 1 ? 1 : 0;
+        if (role == 0) {
+            const long long t0 = clock64();
+            while (vload_u(&gs->gen) == g) {
+                if (vload_i(&gs->err)) {
+                    role = -1;
+                    break;
+                }
+                if (clock64() - t0 > budget) {
+                    atomicCAS(&gs->err, 0, site);
+                    role = -1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_role = role;
+    }
+    __syncthreads();
+    const int role = s_role;
+    if (role == 1) {
+        if (threadIdx.x < 32) lead();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            gs->count = 0;
+            __threadfence();
+            atomicAdd(&gs->gen, 1u);
+        }
+    }
+    return role >= 0;
+}
+
+struct AdvanceLead {
+    BatchInfo *bi;
+    unsigned long long *level_te, *level_cnt;
+    int32_t *level_mode;
+    LevelLists ll;
+    uint32_t pool_cap, list_max;
+    __device__ void operator()() const
+    {
+        level_advance_warp(bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max);
+    }
+};
+struct BwdLead {
+    BatchInfo *bi;
+    __device__ void operator()() const
+    {
+        if (lane_id() == 0 && bi->bd >= 0) bi->bd--;
+    }
+};
+
+// The arrays the loop writes are passed without const/__restrict__, so that
+// no load of them goes through the read-only cache: they change between
+// phases of the one launch.  Levels stop at lmax (the masks allocated): the
+// kernel sets gs->need and the host grows the tables and launches again, the
+// loop resuming from the level state in bi.
+__global__ void __launch_bounds__(BATCH_TPB) k_traverse_persist(
+    Adj a, Adj rv, BatchInfo *bi, uint32_t **tab, uint32_t *seen, uint32_t *msigma, float *mdelta,
+    float *mq, float *mpartial, const uint32_t *reach, uint32_t *ctrs, LevelLists ll,
+    unsigned long long *level_te, unsigned long long *level_cnt, int32_t *level_mode,
+    uint32_t pool_cap, uint32_t list_max, uint64_t n, int lmax, GridSync *gs, long long budget)
+{
+    __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
+    __shared__ uint32_t s_k[BATCH_TPB];
+    const unsigned w0 = threadIdx.x & ~31u;
+    WorkCount<false> none;
+    const AdvanceLead adv{bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max};
+    for (;;) {
+        if (!vload_i(&bi->alive)) break;
+        const int L = vload_i(&bi->cur) + 1;
+        if (L >= lmax) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) gs->need = 1;
+            return;
+        }
+        const uint32_t srcmask = bi->srcmask;
+        if (vload_i(&bi->push_next))
+            fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L, none);
+        else
+            fwd_pull_body(rv, srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, s_u + w0, s_g + w0,
+                          s_k + w0, ll, L, none);
+        if (!grid_barrier(gs, budget, 1, NoLead{})) return;
+        stats_body(n, bi, L, srcmask, tab[L], seen, a.col, rv.col, reach, ll);
+        if (!grid_barrier(gs, budget, 2, adv)) return;
+    }
+    const BwdLead down{bi};
+    for (;;) {
+        const int d = vload_i(&bi->bd);
+        if (d < 0) break;
+        const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
+        if (dmask) {
+            uint32_t lcnt = 0;
+            const uint32_t *lst = level_list(ll, d, lcnt);
+            const uint32_t lheavy = ll.heavy[d];
+            bwd_body(a, dmask, d == bi->dmax, tab[d], tab[d + 1], msigma, mdelta, mq, mpartial, reach,
+                     ctrs + 2 * d + 1, s_u + w0, s_g + w0, lst, lcnt, lheavy, none);
+            if (a.n_heavy && !(lst && lheavy == 0)) {
+                if (!grid_barrier(gs, budget, 3, NoLead{})) return;
+                combine_body(a, dmask, tab[d], msigma, mdelta, mq, mpartial, reach);
+            }
+        }
+        if (!grid_barrier(gs, budget, 4, down)) return;
+    }
+}
+
+// Self-test of the grid barrier: `rounds` barriers, the leader of each adding
+// one to out[0]; block `absent` (if >= 0) never arrives, so the first wait runs
+// out of its budget and every block returns.
+struct CountLead {
+    unsigned *out;
+    __device__ void operator()() const
+    {
+        if (lane_id() == 0) out[0]++;
+    }
+};
+__global__ void __launch_bounds__(BATCH_TPB) k_barrier_selftest(GridSync *gs, int rounds, long long budget,
+                                                                int absent, unsigned *out)
+{
+    if ((int)blockIdx.x == absent) return;
+    const CountLead lead{out};
+    for (int r = 0; r < rounds; r++)
+        if (!grid_barrier(gs, budget, r + 1, lead)) return;
 }
 
 // bc update for the applied pivots in lane order (update_bc, src/cuda_kernels.cu:
@@ -1427,70 +1603,19 @@ static int capture_steps(axbc_ctx *c, int dgrid, int sgrid)
     return AXBC_OK;
 }
 
-// Forward and backward passes of the batch whose roots/p are in c->bi.  The
-// host launches forward level steps in blocks (8, then doubling) and reads
-// the level state once per block; steps past the last level do nothing.
-int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
+// Forward levels and backward depths as launches of the step kernels: CUDA
+// graph replays of one level step, in blocks (profiling and counting: each
+// kernel launched on its own).  *L_out: the first level that discovered
+// nothing.
+static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L_out)
 {
     axbc_graph *g = c->g;
     const uint64_t n = g->n;
     cudaStream_t s = c->stream;
-    const int sgrid = axbc_grid_for(c, BATCH_TPB, 8);
-    const int dgrid = dyn_grid(c);
-    // per-launch mode: profiling events around each kernel, or the counting builds
     const bool prof = c->prof_on || c->count_on;
     unsigned long long *wc = c->count_on ? c->wcount : nullptr;
-    TRY(ensure_level_tables(c));
-    TRY(axbc_batch_levels_alloc(c, 10));
-    if (!prof) TRY(capture_steps(c, dgrid, sgrid));
-
-    // the previous batch's level masks back to zero, then a larger list pool
-    // if that batch ran out of list space
-    if (c->prev_lend >= 2) {
-        k_clean_levels<<<axbc_grid_for(c, 256, 2), 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount,
-                                                              c->lcap, n, 2, c->prev_lend);
-        CU_LAUNCH("k_clean_levels");
-        c->launches++;
-    }
-    c->prev_lend = 0;
-    TRY(axbc_batch_settle(c));
-    if (c->pool_short && c->lpool_cap < 32 * n + 64) {
-        // the larger pool is allocated before the old one goes, so a failed
-        // allocation leaves the context with a usable (smaller) pool
-        const uint32_t ncap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, 32 * n + 64),
-                                                           0xffffffffull);
-        uint32_t *np = nullptr;
-        TRY(axbc_dalloc((void **)&np, (uint64_t)ncap * 4, &c->bytes));
-        CU(cudaStreamSynchronize(s));
-        axbc_dfree(c->lpool);
-        c->lpool = np;
-        c->lpool_cap = ncap;
-        c->pool_short = false;
-        if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
-        if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
-        c->fwd_step_exec = c->bwd_step_exec = nullptr;
-        if (!prof) TRY(capture_steps(c, dgrid, sgrid));
-    }
-    CU(cudaMemsetAsync(c->seen, 0, n * 4, s));
-    CU(cudaMemsetAsync(c->fmask[0], 0, n * 4, s));
-    CU(cudaMemsetAsync(c->fmask[1], 0, n * 4, s));
-    CU(cudaMemsetAsync(c->msigma, 0, n * AXBC_W * 4, s));
-    CU(cudaMemsetAsync(c->ctrs, 0, 2 * AXBC_MAX_LEVELS * 4, s));
-    CU(cudaMemsetAsync(c->lcount, 0, AXBC_MAX_LEVELS * 4, s));
-    CU(cudaMemsetAsync(c->lheavy, 0, AXBC_MAX_LEVELS * 4, s));
     const LevelLists ll = lists_of(c);
     const uint32_t lmax = list_max_of(c);
-    {
-        ProfScope ps(c, KP_LEVEL_STATS, 0);
-        k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
-                                      g->rev.col, g->m, c->push_factor_batch,
-                                      // a factor of 1e30 or more pulls every level
-                                      c->push_factor_batch >= 1e30 ? 0ull : (unsigned long long)(n / 4),
-                                      c->d_level_te,
-                                      c->d_level_cnt, ll, c->lpool_cap, lmax);
-    }
-    CU_LAUNCH("k_batch_init");
-
     const size_t ctl_off = offsetof(BatchInfo, cur);
     const size_t ctl_len = offsetof(BatchInfo, push_factor) - ctl_off;
     const size_t prof_first = c->prof.size();
@@ -1552,6 +1677,7 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         K = std::min(2 * K, 256);
     }
     const int L = c->bi_host->lend, Dmax = c->bi_host->dmax;
+    *L_out = L;
 
     // per-level totals for the byte model of the profiling hooks
     std::vector<unsigned long long> lte, lcnt;
@@ -1624,6 +1750,153 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         }
         CU_LAUNCH("backward levels");
     }
+    return AXBC_OK;
+}
+
+// Whether this batch runs as one persistent launch: always or never when the
+// context says so; otherwise for a batch of at most AXBC_PERSIST_AUTO_WIDTH
+// pivots when the last batch was deep, or -- for the first batch -- when no
+// vertex has more than 64 neighbours (meshes and road-like graphs, whose many
+// levels are narrow).  Measured on 1024^2 and 2048^2 grids: one pivot 14.0 ->
+// 9.9 ms and 19.1 -> 15.8 ms per pass; at 8 pivots even, at 32 pivots the
+// step kernels' fuller grids win.  Counting runs use the step kernels.
+static bool use_persist(axbc_ctx *c, int nsrc)
+{
+    if (c->count_on || c->persist_mode < 0) return false;
+    if (c->persist_mode > 0) return true;
+    if (nsrc > AXBC_PERSIST_AUTO_WIDTH) return false;
+    if (c->last_batch_levels > AXBC_PERSIST_AUTO_LEVELS) return true;
+    return c->last_batch_levels == 0 && c->g->max_deg <= 64;
+}
+
+// The batch's levels in k_traverse_persist: a cooperative launch of every
+// block that fits resident (at most persist_blocks_per_sm per SM).  Level masks
+// are allocated up front for the last batch's depth and grown when the loop
+// asks for more.  *L_out: the first level that discovered nothing.
+static int traverse_persistent(axbc_ctx *c, int *L_out)
+{
+    axbc_graph *g = c->g;
+    cudaStream_t s = c->stream;
+    ALLOC_MISSING(c->gsync, sizeof(GridSync), &c->bytes);
+    int bps = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_traverse_persist, BATCH_TPB, 0));
+    bps = std::min(bps, std::max(1, c->persist_blocks_per_sm));
+    if (bps < 1) {
+        axbc_set_error("persistent level loop: no block of it fits on an SM");
+        return AXBC_ERR_CUDA;
+    }
+    int grid = (c->num_sms > 0 ? c->num_sms : 152) * bps;
+    const LevelLists ll = lists_of(c);
+    const uint32_t lmax_list = list_max_of(c);
+    const uint32_t pool_cap = c->lpool_cap;
+    const uint64_t n = g->n;
+    long long budget = AXBC_BAR_BUDGET;
+    int levels = std::max(16, c->last_batch_levels + 8);
+    GridSync hs;
+    for (;;) {
+        levels = std::min(levels, AXBC_MAX_LEVELS - 2);
+        TRY(axbc_batch_levels_alloc(c, levels));
+        c->prev_lend = levels - 1;  // masks the loop may write, cleared before the next batch
+        CU(cudaMemsetAsync(c->gsync, 0, sizeof(GridSync), s));
+        int lmax = levels;
+        void *args[] = {(void *)&g->fwd, (void *)&g->rev, (void *)&c->bi, (void *)&c->fmtab,
+                        (void *)&c->seen, (void *)&c->msigma, (void *)&c->mdelta, (void *)&c->mq,
+                        (void *)&c->mpartial, (void *)&g->reach, (void *)&c->ctrs, (void *)&ll,
+                        (void *)&c->d_level_te, (void *)&c->d_level_cnt, (void *)&c->d_level_mode,
+                        (void *)&pool_cap, (void *)&lmax_list, (void *)&n, (void *)&lmax,
+                        (void *)&c->gsync, (void *)&budget};
+        {
+            ProfScope ps(c, KP_PERSIST, 0);
+            CU(cudaLaunchCooperativeKernel((const void *)k_traverse_persist, grid, BATCH_TPB, args, 0, s));
+        }
+        CU_LAUNCH("k_traverse_persist");
+        CU(cudaMemcpyAsync(&hs, c->gsync, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        if (hs.err) {
+            axbc_set_error("persistent level loop: a grid barrier wait ran out of its budget (site %d)", hs.err);
+            return AXBC_ERR_TIMEOUT;
+        }
+        if (!hs.need) break;
+        if (levels >= AXBC_MAX_LEVELS - 2) {
+            axbc_set_error("traversal deeper than %d levels", AXBC_MAX_LEVELS - 2);
+            return AXBC_ERR_RANGE;
+        }
+        levels *= 2;
+    }
+    const size_t ctl_off = offsetof(BatchInfo, cur);
+    const size_t ctl_len = offsetof(BatchInfo, push_factor) - ctl_off;
+    CU(cudaMemcpyAsync((char *)c->bi_host + ctl_off, (char *)c->bi + ctl_off, ctl_len, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    *L_out = c->bi_host->lend;
+    return AXBC_OK;
+}
+
+// Forward and backward passes of the batch whose roots/p are in c->bi.  The
+// host launches forward level steps in blocks (8, then doubling) and reads
+// the level state once per block; steps past the last level do nothing.
+int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
+{
+    axbc_graph *g = c->g;
+    const uint64_t n = g->n;
+    cudaStream_t s = c->stream;
+    const int sgrid = axbc_grid_for(c, BATCH_TPB, 8);
+    const int dgrid = dyn_grid(c);
+    // per-launch mode: profiling events around each kernel, or the counting builds
+    const bool prof = c->prof_on || c->count_on;
+    TRY(ensure_level_tables(c));
+    TRY(axbc_batch_levels_alloc(c, 10));
+    if (!prof) TRY(capture_steps(c, dgrid, sgrid));
+
+    // the previous batch's level masks back to zero, then a larger list pool
+    // if that batch ran out of list space
+    if (c->prev_lend >= 2) {
+        k_clean_levels<<<axbc_grid_for(c, 256, 2), 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount,
+                                                              c->lcap, n, 2, c->prev_lend);
+        CU_LAUNCH("k_clean_levels");
+        c->launches++;
+    }
+    c->prev_lend = 0;
+    TRY(axbc_batch_settle(c));
+    if (c->pool_short && c->lpool_cap < 32 * n + 64) {
+        // the larger pool is allocated before the old one goes, so a failed
+        // allocation leaves the context with a usable (smaller) pool
+        const uint32_t ncap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, 32 * n + 64),
+                                                           0xffffffffull);
+        uint32_t *np = nullptr;
+        TRY(axbc_dalloc((void **)&np, (uint64_t)ncap * 4, &c->bytes));
+        CU(cudaStreamSynchronize(s));
+        axbc_dfree(c->lpool);
+        c->lpool = np;
+        c->lpool_cap = ncap;
+        c->pool_short = false;
+        if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
+        if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
+        c->fwd_step_exec = c->bwd_step_exec = nullptr;
+        if (!prof) TRY(capture_steps(c, dgrid, sgrid));
+    }
+    CU(cudaMemsetAsync(c->seen, 0, n * 4, s));
+    CU(cudaMemsetAsync(c->fmask[0], 0, n * 4, s));
+    CU(cudaMemsetAsync(c->fmask[1], 0, n * 4, s));
+    CU(cudaMemsetAsync(c->msigma, 0, n * AXBC_W * 4, s));
+    CU(cudaMemsetAsync(c->ctrs, 0, 2 * AXBC_MAX_LEVELS * 4, s));
+    CU(cudaMemsetAsync(c->lcount, 0, AXBC_MAX_LEVELS * 4, s));
+    CU(cudaMemsetAsync(c->lheavy, 0, AXBC_MAX_LEVELS * 4, s));
+    const LevelLists ll = lists_of(c);
+    const uint32_t lmax = list_max_of(c);
+    {
+        ProfScope ps(c, KP_LEVEL_STATS, 0);
+        k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
+                                      g->rev.col, g->m, c->push_factor_batch,
+                                      // a factor of 1e30 or more pulls every level
+                                      c->push_factor_batch >= 1e30 ? 0ull : (unsigned long long)(n / 4),
+                                      c->d_level_te,
+                                      c->d_level_cnt, ll, c->lpool_cap, lmax);
+    }
+    CU_LAUNCH("k_batch_init");
+
+    int L = 0;
+    if (use_persist(c, nsrc)) TRY(traverse_persistent(c, &L));
+    else TRY(traverse_stepwise(c, nsrc, dgrid, sgrid, &L));
     // the per-pivot level counts and the list-pool flag arrive in the
     // background; the next batch (or a caller that reports them) waits for them
     if (!c->rb_ev) CU(cudaEventCreateWithFlags(&c->rb_ev, cudaEventDisableTiming));
@@ -1869,5 +2142,65 @@ extern "C" int axbc_selftest_division(uint64_t n, uint64_t seed, uint64_t *misma
     axbc_dfree(d);
     *mismatches = h[0];
     if (exact_path) *exact_path = h[1];
+    return AXBC_OK;
+}
+
+// ------------------------------------------------ persistent loop controls
+extern "C" int axbc_ctx_set_persistent(axbc_ctx *c, int mode, int blocks_per_sm)
+{
+    CHECK_ARG(c, "axbc_ctx_set_persistent: null context");
+    CHECK_ARG(mode >= -1 && mode <= 1, "axbc_ctx_set_persistent: mode must be -1, 0 or 1");
+    CHECK_ARG(blocks_per_sm >= 0 && blocks_per_sm <= 8, "axbc_ctx_set_persistent: blocks_per_sm must be in [0, 8]");
+    if (mode > 0) {
+        int dev = 0, coop = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop) {
+            axbc_set_error("axbc_ctx_set_persistent: the device has no cooperative launch");
+            return AXBC_ERR_INVALID;
+        }
+    }
+    c->persist_mode = mode;
+    if (blocks_per_sm > 0) c->persist_blocks_per_sm = blocks_per_sm;
+    return AXBC_OK;
+}
+
+extern "C" int axbc_selftest_grid_barrier(int blocks_per_sm, int rounds, long long budget_cycles,
+                                          int absent_block, int *err_site, uint32_t *leads, float *ms)
+{
+    CHECK_ARG(err_site && leads, "axbc_selftest_grid_barrier: null argument");
+    CHECK_ARG(rounds >= 1 && budget_cycles > 0, "axbc_selftest_grid_barrier: bad rounds or budget");
+    int dev = 0, sms = 0, fit = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_barrier_selftest, BATCH_TPB, 0));
+    CHECK_ARG(blocks_per_sm >= 1 && blocks_per_sm <= fit, "axbc_selftest_grid_barrier: blocks_per_sm does not fit");
+    int grid = sms * blocks_per_sm;
+    CHECK_ARG(absent_block < grid, "axbc_selftest_grid_barrier: absent_block beyond the grid");
+    DBuf gs, out;
+    TRY(gs.alloc(sizeof(GridSync)));
+    TRY(out.alloc(4));
+    CU(cudaMemset(gs.p, 0, sizeof(GridSync)));
+    CU(cudaMemset(out.p, 0, 4));
+    cudaEvent_t a, b;
+    CU(cudaEventCreate(&a));
+    CU(cudaEventCreate(&b));
+    GridSync *gsp = gs.as<GridSync>();
+    unsigned *outp = out.as<unsigned>();
+    void *args[] = {(void *)&gsp, (void *)&rounds, (void *)&budget_cycles, (void *)&absent_block, (void *)&outp};
+    CU(cudaEventRecord(a, 0));
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_barrier_selftest, grid, BATCH_TPB, args, 0, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(b, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) return axbc_cuda_fail(e, "k_barrier_selftest", __FILE__, __LINE__);
+    GridSync h;
+    CU(cudaMemcpy(&h, gs.p, sizeof(h), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(leads, out.p, 4, cudaMemcpyDeviceToHost));
+    *err_site = h.err;
+    if (ms) *ms = t;
     return AXBC_OK;
 }

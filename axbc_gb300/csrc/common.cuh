@@ -163,6 +163,20 @@ struct LaneTargets {
 
 struct SamplerState;  // sampler.cu
 
+// Grid barrier of a cooperative launch (batch.cu): arrival count, generation,
+// and the failure record of a wait that ran out of its budget.
+struct GridSync {
+    unsigned int count;
+    unsigned int gen;
+    int err;   // nonzero: the site of the barrier whose wait ran out
+    int need;  // the persistent forward loop reached the levels allocated
+};
+// batches of at most AXBC_PERSIST_AUTO_WIDTH pivots on graphs whose last batch
+// was deeper than AXBC_PERSIST_AUTO_LEVELS run their levels in one persistent
+// launch
+#define AXBC_PERSIST_AUTO_LEVELS 64
+#define AXBC_PERSIST_AUTO_WIDTH 4
+
 // Kernel kinds timed by the profiling hooks (axbc_ctx_profile).
 enum {
     KP_FWD_PUSH = 0,   // batched forward, push
@@ -175,6 +189,7 @@ enum {
     KP_PLAIN_FWD,      // plain forward level
     KP_PLAIN_BWD,      // plain backward level (+ combine)
     KP_PLAIN_OTHER,    // plain reset / root / reach sum / update
+    KP_PERSIST,        // batched traversal as one persistent cooperative launch
     KP_NKINDS
 };
 
@@ -258,6 +273,11 @@ struct axbc_ctx {
     // captured level steps, accumulating into wcount[kind][field]
     bool count_on = false;
     unsigned long long *wcount = nullptr;  // KP_NKINDS * WC_NFIELDS
+    // persistent level loop: -1 never, 0 when the last batch was deeper than
+    // AXBC_PERSIST_AUTO_LEVELS, 1 always; blocks per SM of its cooperative grid
+    int persist_mode = 0;
+    int persist_blocks_per_sm = 4;
+    struct GridSync *gsync = nullptr;  // its barrier state (device)
     std::vector<cudaEvent_t> ev_pool;
     double level_te_prev = 0;  // degree sum of the previous level's new vertices
     std::vector<double> level_te;

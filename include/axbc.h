@@ -338,8 +338,9 @@ int axbc_ctx_sync(axbc_ctx *ctx);
  * 20 bytes per vertex per pivot for the update).  Kinds:
  * 0 batched forward push, 1 batched forward pull, 2 level bookkeeping,
  * 3 batched backward, 4 heavy-vertex combine, 5 bc update, 6 sampler,
- * 7 plain forward, 8 plain backward, 9 plain other. */
-#define AXBC_PROF_KINDS 10
+ * 7 plain forward, 8 plain backward, 9 plain other, 10 a whole batched
+ * pass in one persistent launch. */
+#define AXBC_PROF_KINDS 11
 int axbc_ctx_profile(axbc_ctx *ctx, int enable);
 /* per kind: total milliseconds, launches, algorithmic bytes; clears the records */
 int axbc_ctx_profile_read(axbc_ctx *ctx, double *ms, uint64_t *count, double *bytes, int nkinds);
@@ -350,6 +351,27 @@ int axbc_ctx_profile_records(axbc_ctx *ctx, int32_t *kinds, int32_t *tags, float
                              uint64_t cap, uint64_t *count);
 /* kernels launched by this context since it was created */
 int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
+
+/* ---- persistent level loop ----
+ * A batched pass normally launches four kernels per forward level and two or
+ * three per backward depth.  On graphs of many narrow levels it can instead
+ * run as one cooperative launch (all blocks resident, a bounded grid barrier
+ * between phases).  mode 1 always, -1 never, 0 (default) for batches of at
+ * most 4 pivots when the context's last batch was deeper than 64 levels or,
+ * for its first batch, when no vertex has more than 64 neighbours.
+ * blocks_per_sm: blocks of the cooperative grid per SM (0 keeps the current
+ * setting, default 4).  Results
+ * are the same bits either way.  A barrier wait that runs out of its budget
+ * (about 4 s) ends the pass with AXBC_ERR_TIMEOUT.  No counterpart in the
+ * reference (its host synchronises every level). */
+int axbc_ctx_set_persistent(axbc_ctx *ctx, int mode, int blocks_per_sm);
+/* Self-test of that grid barrier on the current device: `rounds` barriers
+ * over blocks_per_sm blocks per SM; block absent_block (>= 0) never arrives,
+ * so the first wait runs out of budget_cycles (SM clock cycles) and every
+ * block returns.  *err_site: 0, or the 1-based barrier whose wait ran out;
+ * *leads: barriers completed; *ms: the launch's time. */
+int axbc_selftest_grid_barrier(int blocks_per_sm, int rounds, long long budget_cycles, int absent_block,
+                               int *err_site, uint32_t *leads, float *ms);
 
 /* ---- work counting ----
  * With counting on, batched passes launch counting builds of the forward
