@@ -13,7 +13,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libaxbc_gb300.so")
-MAX_BATCH = 32
+MAX_BATCH = 64
 _LIB = None
 
 

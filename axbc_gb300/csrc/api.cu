@@ -237,8 +237,10 @@ extern "C" int axbc_ctx_destroy(axbc_ctx *c)
     axbc_dfree(c->lcount);
     axbc_dfree(c->lcap);
     axbc_dfree(c->lheavy);
-    if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
-    if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
+    for (int i = 0; i < 2; i++) {
+        if (c->fwd_step_exec[i]) cudaGraphExecDestroy(c->fwd_step_exec[i]);
+        if (c->bwd_step_exec[i]) cudaGraphExecDestroy(c->bwd_step_exec[i]);
+    }
     axbc_dfree(c->mpartial);
     axbc_dfree(c->bi);
     if (c->bi_host) cudaFreeHost(c->bi_host);

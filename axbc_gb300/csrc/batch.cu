@@ -14,16 +14,75 @@
 
 #define BATCH_TPB 256
 
-static __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * AXBC_W; }
+// K: 32-bit mask words per vertex.  K = 1: a pass of up to 32 pivots, lane s
+// of a warp owns pivot s.  K = 2: up to 64 pivots, lane l owns pivots l and
+// l + 32 (its two "halves"), masks are 64-bit, per-pivot rows hold 64 values
+// and one adjacency entry and one mask load serve all 64 pivots.
+template <int K> struct MaskOf;
+template <> struct MaskOf<1> {
+    typedef uint32_t T;
+};
+template <> struct MaskOf<2> {
+    typedef unsigned long long T;
+};
 
-// resident blocks per SM the pull and backward kernels are compiled for
-// (their register budgets)
+template <int K> __device__ __forceinline__ uint64_t row_base(uint64_t v) { return v * (uint64_t)(AXBC_W * K); }
+
+// bit of this lane's pivot of half h (a 32-bit mask has only half 0)
+__device__ __forceinline__ bool pbit(uint32_t m, int) { return (m >> lane_id()) & 1u; }
+__device__ __forceinline__ bool pbit(unsigned long long m, int h)
+{
+    return (uint32_t)(m >> (32 * h)) >> lane_id() & 1u;
+}
+template <class M> __device__ __forceinline__ M lane_mask(int s) { return (M)1 << s; }
+
+__device__ __forceinline__ uint32_t warp_or(uint32_t m) { return __reduce_or_sync(FULL_MASK, m); }
+__device__ __forceinline__ unsigned long long warp_or(unsigned long long m)
+{
+    const uint32_t lo = __reduce_or_sync(FULL_MASK, (uint32_t)m);
+    const uint32_t hi = __reduce_or_sync(FULL_MASK, (uint32_t)(m >> 32));
+    return (unsigned long long)lo | ((unsigned long long)hi << 32);
+}
+
+// A warp stages the masks of a 32-position chunk in shared memory as K
+// arrays of 32 words, one per 32-bit half (sg + 32 h), so that a half's
+// consumer holds 32-bit words only.
+template <int K, class M> __device__ __forceinline__ void stage_mask(uint32_t *sg, M m)
+{
+    sg[lane_id()] = (uint32_t)m;
+    if (K == 2) sg[32 + lane_id()] = (uint32_t)((unsigned long long)m >> 32);
+}
+template <int K> __device__ __forceinline__ typename MaskOf<K>::T staged_mask(const uint32_t *sg, int i)
+{
+    typedef typename MaskOf<K>::T M;
+    if (K == 1) return (M)sg[i];
+    return (M)((unsigned long long)sg[i] | ((unsigned long long)sg[32 + i] << 32));
+}
+
+// eight staged words of group g (16-byte shared loads)
+__device__ __forceinline__ void load8u(const uint32_t *su, int g, uint32_t u[8])
+{
+    const uint4 *p = reinterpret_cast<const uint4 *>(su) + 2 * g;
+    const uint4 a = p[0], b = p[1];
+    u[0] = a.x, u[1] = a.y, u[2] = a.z, u[3] = a.w, u[4] = b.x, u[5] = b.y, u[6] = b.z, u[7] = b.w;
+}
+
+// resident blocks per SM the kernels are compiled for (their register
+// budgets); the backward runs 32 pivots at a time at either width
 #ifndef AXBC_PULL_MIN_BLOCKS
 #define AXBC_PULL_MIN_BLOCKS 6
 #endif
 #ifndef AXBC_BWD_MIN_BLOCKS
 #define AXBC_BWD_MIN_BLOCKS 8
 #endif
+#ifndef AXBC_PUSH_MIN_BLOCKS2
+#define AXBC_PUSH_MIN_BLOCKS2 5
+#endif
+#ifndef AXBC_PULL_MIN_BLOCKS2
+#define AXBC_PULL_MIN_BLOCKS2 4
+#endif
+#define PUSH_BLOCKS(K) ((K) == 1 ? 8 : AXBC_PUSH_MIN_BLOCKS2)
+#define PULL_BLOCKS(K) ((K) == 1 ? AXBC_PULL_MIN_BLOCKS : AXBC_PULL_MIN_BLOCKS2)
 
 // Per-level vertex lists: the vertices whose level-L mask is nonzero, appended
 // by the forward kernels that set the mask.  A level whose list would exceed
@@ -42,15 +101,17 @@ struct LevelLists {
 // are cleared with memsets): a level whose list was stored has nonzero
 // entries only at its listed vertices; an overflowed level is cleared whole.
 // The grid walks the levels in order, all blocks sharing each level.
+template <int K>
 __global__ void k_clean_levels(uint32_t *const *__restrict__ tab, const uint32_t *__restrict__ pool,
                                const uint32_t *__restrict__ lstart,
                                const uint32_t *__restrict__ lcount,
                                const uint32_t *__restrict__ lcap, uint64_t n, int first, int last)
 {
+    typedef typename MaskOf<K>::T M;
     const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint64_t nt = (uint64_t)gridDim.x * blockDim.x;
     for (int L = first; L <= last; L++) {
-        uint32_t *f = tab[L];
+        M *f = reinterpret_cast<M *>(tab[L]);
         const uint32_t cnt = lcount[L];
         if (cnt <= lcap[L]) {
             const uint32_t *lst = pool + lstart[L];
@@ -61,8 +122,10 @@ __global__ void k_clean_levels(uint32_t *const *__restrict__ tab, const uint32_t
     }
 }
 
-// roots: depth 0, sigma 1 (set_mlp_cuda, src/cuda_kernels.cu:862-876)
-__global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t *fmask0, uint32_t *seen,
+// roots: depth 0, sigma 1 (set_mlp_cuda, src/cuda_kernels.cu:862-876); one
+// warp, lane l setting up pivots l + 32 h
+template <int K>
+__global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t *fmask0_, uint32_t *seen_,
                              uint32_t *msigma, const uint32_t *__restrict__ col,
                              const uint32_t *__restrict__ rcol, unsigned long long m,
                              double push_factor, unsigned long long push_min,
@@ -70,10 +133,12 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
                              unsigned long long *level_cnt, LevelLists ll, uint32_t pool_cap,
                              uint32_t list_max)
 {
-    const int s = threadIdx.x;
-    if (s == 0) {
+    typedef typename MaskOf<K>::T M;
+    M *fmask0 = reinterpret_cast<M *>(fmask0_), *seen = reinterpret_cast<M *>(seen_);
+    const int l = threadIdx.x;
+    if (l == 0) {
         bi->nsrc = nsrc;
-        bi->srcmask = nsrc >= 32 ? FULL_MASK : ((1u << nsrc) - 1u);
+        bi->srcmask = nsrc >= 64 ? ~0ull : ((1ull << nsrc) - 1ull);
         bi->applymask = bi->srcmask;
         bi->depth0mask = 0;
         bi->H = H;
@@ -87,41 +152,50 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
         bi->any_new = 0;
         bi->pool_short = 0;
     }
-    if (s < AXBC_W) {
+    unsigned long long fd = 0, rd = 0;
+    uint32_t nroots = 0, heavy_roots = 0;
+    const uint32_t rt0 = l < nsrc ? bi->root[l] : 0xffffffffu;
+#pragma unroll
+    for (int h = 0; h < K; h++) {
+        const int s = l + 32 * h;
         bi->Ls[s] = 0;
         bi->lvl_new[s] = 0;
-    }
-    unsigned long long fd = 0, rd = 0;
-    if (s < nsrc) {
-        const uint32_t v = bi->root[s];
-        atomicOr(&fmask0[v], 1u << s);
-        atomicOr(&seen[v], 1u << s);
-        msigma[row_base(v) + s] = 1;
-        bi->nvis[s] = 1;
-        bi->rsum[s] = 0;
-        bi->te[s] = col[v + 1] - col[v];
-        fd = col[v + 1] - col[v];
-        rd = rcol[v + 1] - rcol[v];
-    } else if (s < AXBC_W) {
-        bi->nvis[s] = 0;
-        bi->rsum[s] = 0;
-        bi->te[s] = 0;
+        bi->lane_bc[s] = bc;
+        if (s < nsrc) {
+            const uint32_t v = bi->root[s];
+            atomicOr(&fmask0[v], lane_mask<M>(s));
+            atomicOr(&seen[v], lane_mask<M>(s));
+            msigma[row_base<K>(v) + s] = 1;
+            bi->nvis[s] = 1;
+            bi->rsum[s] = 0;
+            bi->te[s] = col[v + 1] - col[v];
+            fd += col[v + 1] - col[v];
+            rd += rcol[v + 1] - rcol[v];
+        } else {
+            bi->nvis[s] = 0;
+            bi->rsum[s] = 0;
+            bi->te[s] = 0;
+        }
+        // the level-0 list: each root once (lanes of different runs may share one)
+        const uint32_t rt = s < nsrc ? bi->root[s] : 0xffffffffu;
+        const uint32_t same = __match_any_sync(FULL_MASK, rt);
+        bool first = s < nsrc && (__ffs(same) - 1) == l;
+        if (h == 1) {
+            bool dup = false;
+            for (int j = 0; j < 32; j++) dup |= __shfl_sync(FULL_MASK, rt0, j) == rt;
+            first = first && !dup;
+        }
+        const uint32_t firsts = __ballot_sync(FULL_MASK, first);
+        if (first) ll.pool[nroots + __popc(firsts & ((1u << l) - 1u))] = rt;
+        nroots += __popc(firsts);
+        heavy_roots += __popc(__ballot_sync(FULL_MASK, first && col[rt + 1] - col[rt] > AXBC_SPAN));
     }
     for (int o = 16; o; o >>= 1) {
         fd += __shfl_xor_sync(FULL_MASK, fd, o);
         rd += __shfl_xor_sync(FULL_MASK, rd, o);
     }
-    // the level-0 list: each root once (lanes of different runs may share one)
-    const uint32_t rt = s < nsrc ? bi->root[s] : 0xffffffffu;
-    const uint32_t same = __match_any_sync(FULL_MASK, rt);
-    const bool first = s < nsrc && (__ffs(same) - 1) == s;
-    const uint32_t firsts = __ballot_sync(FULL_MASK, first);
-    if (first) ll.pool[__popc(firsts & ((1u << s) - 1u))] = rt;
-    const uint32_t nroots = __popc(firsts);
-    const uint32_t heavy_roots = __popc(__ballot_sync(FULL_MASK, first && col[rt + 1] - col[rt] > AXBC_SPAN));
-    if (s == 0) ll.heavy[0] = heavy_roots;
-    if (s < AXBC_W) bi->lane_bc[s] = bc;
-    if (s == 0) {
+    if (l == 0) {
+        ll.heavy[0] = heavy_roots;
         // a vertex counts as unvisited until every pivot has seen it: with one
         // pivot its root is fully seen at once
         const unsigned long long unvis = nsrc == 1 ? m - rd : m;
@@ -200,38 +274,46 @@ __device__ __forceinline__ const uint32_t *level_list(const LevelLists &ll, int 
 // Forward level L, push from the vertices of depth L-1: for each neighbour u
 // and each pivot s with v at depth L-1 and u unseen, sigma_s[u] += sigma_s[v]
 // and bit s joins u's level-L mask.  Atomics are fire-and-forget reductions.
-template <class WC>
-__device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, uint32_t b0,
-                                          uint32_t b1, const uint32_t *__restrict__ seen,
-                                          uint32_t *fcur, uint32_t *msigma, const LevelLists &ll,
-                                          int L, WC &wc)
+template <int K, class WC>
+__device__ __forceinline__ void push_span(const Adj &a, uint32_t v, typename MaskOf<K>::T f, uint32_t b0,
+                                          uint32_t b1, const typename MaskOf<K>::T *__restrict__ seen,
+                                          typename MaskOf<K>::T *fcur, uint32_t *msigma,
+                                          const LevelLists &ll, int L, WC &wc)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
-    const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
-    if ((f >> lane) & 1u) wc.add(WC_BYTES, 4);
+    uint32_t sig[K];
+#pragma unroll
+    for (int h = 0; h < K; h++) {
+        sig[h] = pbit(f, h) ? msigma[row_base<K>(v) + 32 * h + lane] : 0u;
+        if (pbit(f, h)) wc.add(WC_BYTES, 4);
+    }
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
-        uint32_t u = 0, nm = 0;
+        uint32_t u = 0;
+        M nm = 0;
         if (e < b1) {
             u = a.row[e];
             nm = f & ~seen[u];
             wc.add(WC_ENTRIES, 1);
-            wc.add(WC_BYTES, 8);  // adjacency entry, seen mask
+            wc.add(WC_BYTES, 4 + 4 * K);  // adjacency entry, seen mask
         }
-        const uint32_t old = nm ? atomicOr(&fcur[u], nm) : 1u;
-        if (nm) wc.add(WC_BYTES, old == 0u ? 8 : 4);  // level mask, list entry
-        list_append(ll, L, old == 0u, u);
+        const M old = nm ? atomicOr(&fcur[u], nm) : (M)1;
+        if (nm) wc.add(WC_BYTES, old == 0 ? 4 + 4 * K : 4 * K);  // level mask, list entry
+        list_append(ll, L, old == 0, u);
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
             const int j = __ffs(act) - 1;
             act &= act - 1;
             const uint32_t uj = __shfl_sync(FULL_MASK, u, j);
-            const uint32_t mj = __shfl_sync(FULL_MASK, nm, j);
-            if ((mj >> lane) & 1u) {
-                atomicAdd(&msigma[row_base(uj) + lane], sig);
-                wc.add(WC_PAIRS, 1);
-                wc.add(WC_BYTES, 4);
-            }
+            const M mj = __shfl_sync(FULL_MASK, nm, j);
+#pragma unroll
+            for (int h = 0; h < K; h++)
+                if (pbit(mj, h)) {
+                    atomicAdd(&msigma[row_base<K>(uj) + 32 * h + lane], sig[h]);
+                    wc.add(WC_PAIRS, 1);
+                    wc.add(WC_BYTES, 4);
+                }
         }
     }
 }
@@ -241,11 +323,13 @@ __device__ __forceinline__ void push_span(const Adj &a, uint32_t v, uint32_t f, 
 // lists 32 positions at a time, so a chunk of low-degree vertices costs one
 // pass instead of one pass per vertex.  Lane e finds its vertex by a binary
 // search over the inclusive degree prefix held across the lanes.
-template <class WC>
-__device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, uint32_t f_l,
-                                             const uint32_t *__restrict__ seen, uint32_t *fcur,
-                                             uint32_t *msigma, const LevelLists &ll, int L, WC &wc)
+template <int K, class WC>
+__device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, typename MaskOf<K>::T f_l,
+                                             const typename MaskOf<K>::T *__restrict__ seen,
+                                             typename MaskOf<K>::T *fcur, uint32_t *msigma,
+                                             const LevelLists &ll, int L, WC &wc)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
     uint32_t b = 0, d = 0;
     if (f_l) {
@@ -268,49 +352,58 @@ __device__ __forceinline__ void push_light32(const Adj &a, uint32_t v_l, uint32_
         for (int step = 16; step; step >>= 1)
             if (__shfl_sync(FULL_MASK, inc, k + step - 1) <= e) k += step;
         const uint32_t pk = __shfl_sync(FULL_MASK, shift, k) + e;
-        const uint32_t fk = __shfl_sync(FULL_MASK, f_l, k);
-        uint32_t u = 0, nm = 0;
+        const M fk = __shfl_sync(FULL_MASK, f_l, k);
+        uint32_t u = 0;
+        M nm = 0;
         if (e < total) {
             u = a.row[pk];
             nm = fk & ~seen[u];
             wc.add(WC_ENTRIES, 1);
-            wc.add(WC_BYTES, 8);  // adjacency entry, seen mask
+            wc.add(WC_BYTES, 4 + 4 * K);  // adjacency entry, seen mask
         }
-        const uint32_t old = nm ? atomicOr(&fcur[u], nm) : 1u;
-        if (nm) wc.add(WC_BYTES, old == 0u ? 8 : 4);  // level mask, list entry
-        list_append(ll, L, old == 0u, u);
+        const M old = nm ? atomicOr(&fcur[u], nm) : (M)1;
+        if (nm) wc.add(WC_BYTES, old == 0 ? 4 + 4 * K : 4 * K);  // level mask, list entry
+        list_append(ll, L, old == 0, u);
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
             // up to 4 edges: gather the parents' sigma rows, then add
-            uint32_t uu[4], mm[4], sg[4];
+            uint32_t uu[4], sg[4][K];
+            M mm[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int j = act ? __ffs(act) - 1 : 0;
                 const bool ok = act != 0;
                 act &= act - 1;
                 uu[q] = __shfl_sync(FULL_MASK, u, j);
-                mm[q] = ok ? __shfl_sync(FULL_MASK, nm, j) : 0u;
+                const M mj = __shfl_sync(FULL_MASK, nm, j);
+                mm[q] = ok ? mj : (M)0;
                 const uint32_t vj = __shfl_sync(FULL_MASK, v_l, __shfl_sync(FULL_MASK, k, j));
-                sg[q] = ((mm[q] >> lane) & 1u) ? msigma[row_base(vj) + lane] : 0u;
+#pragma unroll
+                for (int h = 0; h < K; h++)
+                    sg[q][h] = pbit(mm[q], h) ? msigma[row_base<K>(vj) + 32 * h + lane] : 0u;
             }
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if ((mm[q] >> lane) & 1u) {
-                    atomicAdd(&msigma[row_base(uu[q]) + lane], sg[q]);
-                    wc.add(WC_GATHERS, 1);
-                    wc.add(WC_PAIRS, 1);
-                    wc.add(WC_BYTES, 8);  // parent's path count, child's sum
-                }
+#pragma unroll
+                for (int h = 0; h < K; h++)
+                    if (pbit(mm[q], h)) {
+                        atomicAdd(&msigma[row_base<K>(uu[q]) + 32 * h + lane], sg[q][h]);
+                        wc.add(WC_GATHERS, 1);
+                        wc.add(WC_PAIRS, 1);
+                        wc.add(WC_BYTES, 8);  // parent's path count, child's sum
+                    }
         }
     }
 }
 
-template <class WC>
-__device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__restrict__ fprev,
-                                              uint32_t *fcur, const uint32_t *__restrict__ seen,
+template <int K, class WC>
+__device__ __forceinline__ void fwd_push_body(const Adj &a, const typename MaskOf<K>::T *__restrict__ fprev,
+                                              typename MaskOf<K>::T *fcur,
+                                              const typename MaskOf<K>::T *__restrict__ seen,
                                               uint32_t *msigma, uint32_t *ctr, const LevelLists &ll,
                                               int L, WC &wc)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
     uint32_t lcnt = 0;
     const uint32_t *lst = level_list(ll, L - 1, lcnt);  // the frontier, when stored
@@ -324,34 +417,36 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
         if (t >= nu) break;
         if (t < nhi) {
             const uint32_t v = a.hitem_v[t];
-            const uint32_t f = fprev[v];
-            if (lane == 0) wc.add(WC_BYTES, 4);
+            const M f = fprev[v];
+            if (lane == 0) wc.add(WC_BYTES, 4 * K);
             if (!f) continue;
             const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
-            push_span(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma, ll, L, wc);
+            push_span<K>(a, v, f, b0, min(a.col[v + 1], b0 + AXBC_SPAN), seen, fcur, msigma, ll, L, wc);
             continue;
         }
         if (lst) {
             const uint32_t i = (uint32_t)(t - nhi) * ent + lane;
-            uint32_t v_l = 0, f_l = 0;
+            uint32_t v_l = 0;
+            M f_l = 0;
             if (lane < ent && i < lcnt) {
                 v_l = lst[i];
                 if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fprev[v_l];
-                wc.add(WC_BYTES, 8);  // list entry, level mask
+                wc.add(WC_BYTES, 4 + 4 * K);  // list entry, level mask
             }
-            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L, wc);
+            push_light32<K>(a, v_l, f_l, seen, fcur, msigma, ll, L, wc);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
         for (uint64_t lt = l0; lt < l0 + LIGHT_PER_UNIT && lt < a.n_ltask; lt++) {
             const uint32_t beg = a.ltask[lt], cnt = a.ltask[lt + 1] - beg;
-            uint32_t v_l = 0, f_l = 0;
+            uint32_t v_l = 0;
+            M f_l = 0;
             if (lane < cnt) {
                 v_l = a.order[beg + lane];
                 f_l = fprev[v_l];
-                wc.add(WC_BYTES, 4);  // level mask
+                wc.add(WC_BYTES, 4 * K);  // level mask
             }
-            push_light32(a, v_l, f_l, seen, fcur, msigma, ll, L, wc);
+            push_light32<K>(a, v_l, f_l, seen, fcur, msigma, ll, L, wc);
         }
     }
 }
@@ -359,52 +454,53 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const uint32_t *__re
 // Forward level L, pull into vertex u for the pivots `ns` that have not seen
 // it: sum sigma_s over every in-neighbour at depth L-1 from pivot s (u32 sums:
 // any order gives the same bits).  The positions of a 32-wide chunk are staged
-// in shared memory; each 8-position group with a hit issues its eight gathers
-// before any is consumed.
-template <class WC>
-__device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32_t b0, uint32_t b1,
-                                              const uint32_t *__restrict__ fprev,
-                                              const uint32_t *__restrict__ msigma, uint32_t *su,
-                                              uint32_t *sg, uint32_t &acc, WC &wc)
+// in shared memory; each 8-position group with a hit issues its gathers (8 per
+// half) before any is consumed.
+template <int K, class WC>
+__device__ __forceinline__ typename MaskOf<K>::T pull_span(const Adj &rv, typename MaskOf<K>::T ns, uint32_t b0,
+                                                           uint32_t b1,
+                                                           const typename MaskOf<K>::T *__restrict__ fprev,
+                                                           const uint32_t *__restrict__ msigma, uint32_t *su,
+                                                           uint32_t *sg, uint32_t acc[K], WC &wc)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
-    const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
-    const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
-    uint32_t found = 0;
-    acc = 0;
+    M found = 0;
+#pragma unroll
+    for (int h = 0; h < K; h++) acc[h] = 0;
     // the next chunk's adjacency entries load while this chunk is consumed
     uint32_t vn = b0 + lane < b1 ? rv.row[b0 + lane] : 0u;
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
         const uint32_t v = vn;
         vn = e + 32 < b1 ? rv.row[e + 32] : 0u;
-        const uint32_t fm = e < b1 ? fprev[v] & ns : 0u;
+        const M fm = e < b1 ? fprev[v] & ns : (M)0;
         if (e < b1) {
             wc.add(WC_ENTRIES, 1);
-            wc.add(WC_GATHERS, __popc(fm));
-            wc.add(WC_BYTES, 8 + 4 * __popc(fm));  // adjacency entry, level mask, parents' counts
+            wc.add(WC_GATHERS, __popcll((unsigned long long)fm));
+            wc.add(WC_BYTES, 4 + 4 * K + 4 * __popcll((unsigned long long)fm));  // entry, mask, parents' counts
         }
         const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
-        found |= __reduce_or_sync(FULL_MASK, fm);
+        found |= warp_or(fm);
         su[lane] = v;
-        sg[lane] = fm;
+        stage_mask<K>(sg, fm);
         __syncwarp();
 #pragma unroll 1
         for (int g = 0; g < 4; g++) {
             if (!((act >> (8 * g)) & 0xffu)) continue;
-            uint32_t x[8];
+            uint32_t u[8];
+            load8u(su, g, u);
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const uint4 ua = su4[2 * g + h], ga = sg4[2 * g + h];
-                const uint32_t u[4] = {ua.x, ua.y, ua.z, ua.w};
-                const uint32_t m[4] = {ga.x, ga.y, ga.z, ga.w};
+            for (int h = 0; h < K; h++) {
+                uint32_t m[8], x[8];
+                load8u(sg + 32 * h, g, m);
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    x[4 * h + q] = ((m[q] >> lane) & 1u) ? msigma[row_base(u[q]) + lane] : 0u;
+                for (int q = 0; q < 8; q++)
+                    x[q] = ((m[q] >> lane) & 1u) ? msigma[row_base<K>(u[q]) + 32 * h + lane] : 0u;
+#pragma unroll
+                for (int q = 0; q < 8; q++) acc[h] += x[q];
             }
-#pragma unroll
-            for (int q = 0; q < 8; q++) acc += x[q];
         }
         __syncwarp();
     }
@@ -417,11 +513,14 @@ __device__ __forceinline__ uint32_t pull_span(const Adj &rv, uint32_t ns, uint32
 // held across the lanes.  Positions arrive grouped by vertex, so one running
 // sum per lane (pivot) is written out whenever the vertex changes.  Returns the
 // discovered mask of the lane's own vertex.
-template <class WC>
-__device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, uint32_t ns_l,
-                                                 const uint32_t *__restrict__ fprev, uint32_t *msigma,
-                                                 uint32_t *su, uint32_t *sg, uint32_t *sk, WC &wc)
+template <int K, class WC>
+__device__ __forceinline__ typename MaskOf<K>::T pull_light32(const Adj &rv, uint32_t u_l,
+                                                              typename MaskOf<K>::T ns_l,
+                                                              const typename MaskOf<K>::T *__restrict__ fprev,
+                                                              uint32_t *msigma, uint32_t *su,
+                                                              uint32_t *sg, uint32_t *sk, WC &wc)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
     uint32_t b = 0, d = 0;
     if (ns_l) {
@@ -437,8 +536,19 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
     }
     const uint32_t total = __shfl_sync(FULL_MASK, inc, 31);
     const uint32_t shift = b - (inc - d);  // position of concatenated index e: shift_k + e
-    uint32_t mine = 0, acc = 0, fo = 0;
+    M mine = 0, fo = 0;
+    uint32_t acc[K];
+#pragma unroll
+    for (int h = 0; h < K; h++) acc[h] = 0;
     int cur = -1;
+    // the finished running sums of vertex `cur` go to its row
+    auto flush = [&]() {
+        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
+#pragma unroll
+        for (int h = 0; h < K; h++)
+            if (pbit(fo, h)) msigma[row_base<K>(uc) + 32 * h + lane] = acc[h];
+        if ((int)lane == cur) mine = fo;
+    };
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t e = base + lane;
         uint32_t k = 0;
@@ -446,91 +556,88 @@ __device__ __forceinline__ uint32_t pull_light32(const Adj &rv, uint32_t u_l, ui
         for (int step = 16; step; step >>= 1)
             if (__shfl_sync(FULL_MASK, inc, k + step - 1) <= e) k += step;
         const uint32_t pk = __shfl_sync(FULL_MASK, shift, k) + e;
-        const uint32_t nk = __shfl_sync(FULL_MASK, ns_l, k);
-        uint32_t v = 0, fm = 0;
+        const M nk = __shfl_sync(FULL_MASK, ns_l, k);
+        uint32_t v = 0;
+        M fm = 0;
         if (e < total) {
             v = rv.row[pk];
             fm = fprev[v] & nk;
             wc.add(WC_ENTRIES, 1);
-            wc.add(WC_GATHERS, __popc(fm));
-            wc.add(WC_BYTES, 8 + 4 * __popc(fm));  // adjacency entry, level mask, parents' counts
+            wc.add(WC_GATHERS, __popcll((unsigned long long)fm));
+            wc.add(WC_BYTES, 4 + 4 * K + 4 * __popcll((unsigned long long)fm));  // entry, mask, parents' counts
         }
         const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
         su[lane] = v;
-        sg[lane] = fm;
+        stage_mask<K>(sg, fm);
         sk[lane] = k;
         __syncwarp();
-        const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
-        const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
 #pragma unroll 1
         for (int g = 0; g < 4; g++) {
             if (!((act >> (8 * g)) & 0xffu)) continue;
-            uint32_t x[8], mor = 0;
+            uint32_t u4[8];
+            load8u(su, g, u4);
+            uint32_t x[K][8];
+            M mor = 0;
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const uint4 uu = su4[2 * g + h], mm = sg4[2 * g + h];
-                const uint32_t u4[4] = {uu.x, uu.y, uu.z, uu.w};
-                const uint32_t m4[4] = {mm.x, mm.y, mm.z, mm.w};
+            for (int h = 0; h < K; h++) {
+                uint32_t m4[8], mh = 0;
+                load8u(sg + 32 * h, g, m4);
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    x[4 * h + q] = ((m4[q] >> lane) & 1u) ? msigma[row_base(u4[q]) + lane] : 0u;
-                    mor |= m4[q];
+                for (int q = 0; q < 8; q++) {
+                    x[h][q] = ((m4[q] >> lane) & 1u) ? msigma[row_base<K>(u4[q]) + 32 * h + lane] : 0u;
+                    mh |= m4[q];
                 }
+                mor |= (M)((unsigned long long)mh << (32 * h));
             }
             const int k0 = (int)sk[8 * g], k7 = (int)sk[8 * g + 7];
             if (k0 == k7) {
                 // all eight positions belong to one vertex (k is nondecreasing)
                 if (k0 != cur) {
-                    if (cur >= 0) {
-                        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
-                        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
-                        if ((int)lane == cur) mine = fo;
-                    }
+                    if (cur >= 0) flush();
                     cur = k0;
-                    acc = 0;
+#pragma unroll
+                    for (int h = 0; h < K; h++) acc[h] = 0;
                     fo = 0;
                 }
-                acc += ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
+#pragma unroll
+                for (int h = 0; h < K; h++)
+                    acc[h] += ((x[h][0] + x[h][1]) + (x[h][2] + x[h][3])) + ((x[h][4] + x[h][5]) + (x[h][6] + x[h][7]));
                 fo |= mor;
                 continue;
             }
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                const uint32_t m = sg[8 * g + q];
-                if (!m) continue;
+                const M mq = staged_mask<K>(sg, 8 * g + q);
+                if (!mq) continue;
                 const int kq = (int)sk[8 * g + q];
                 if (kq != cur) {
-                    if (cur >= 0) {
-                        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
-                        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
-                        if ((int)lane == cur) mine = fo;
-                    }
+                    if (cur >= 0) flush();
                     cur = kq;
-                    acc = 0;
+#pragma unroll
+                    for (int h = 0; h < K; h++) acc[h] = 0;
                     fo = 0;
                 }
-                acc += x[q];
-                fo |= m;
+#pragma unroll
+                for (int h = 0; h < K; h++) acc[h] += x[h][q];
+                fo |= mq;
             }
         }
         __syncwarp();
     }
-    if (cur >= 0) {
-        const uint32_t uc = __shfl_sync(FULL_MASK, u_l, cur);
-        if ((fo >> lane) & 1u) msigma[row_base(uc) + lane] = acc;
-        if ((int)lane == cur) mine = fo;
-    }
+    if (cur >= 0) flush();
     return mine;
 }
 
-template <class WC>
-__device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
-                                              const uint32_t *__restrict__ fprev, uint32_t *fcur,
-                                              const uint32_t *__restrict__ seen, uint32_t *msigma,
+template <int K, class WC>
+__device__ __forceinline__ void fwd_pull_body(const Adj &rv, typename MaskOf<K>::T srcmask,
+                                              const typename MaskOf<K>::T *__restrict__ fprev,
+                                              typename MaskOf<K>::T *fcur,
+                                              const typename MaskOf<K>::T *__restrict__ seen, uint32_t *msigma,
                                               uint32_t *ctr, uint32_t *su, uint32_t *sg,
                                               uint32_t *sk, const LevelLists &ll, int L, WC &wc)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
     const uint64_t nhi = rv.n_heavy_items, nu = n_units(rv);
     if (warp_global() >= nu) return;  // fewer units than warps: no contention
@@ -539,40 +646,43 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
         if (t >= nu) break;
         if (t < nhi) {
             const uint32_t u = rv.hitem_v[t];
-            const uint32_t ns = srcmask & ~seen[u];
-            if (lane == 0) wc.add(WC_BYTES, 4);  // seen mask
+            const M ns = srcmask & ~seen[u];
+            if (lane == 0) wc.add(WC_BYTES, 4 * K);  // seen mask
             if (!ns) continue;
             const uint32_t b0 = rv.col[u] + rv.hitem_k[t] * AXBC_SPAN;
-            uint32_t acc;
-            const uint32_t nm =
-                pull_span(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg, acc, wc);
-            if ((nm >> lane) & 1u) {
-                atomicAdd(&msigma[row_base(u) + lane], acc);
-                wc.add(WC_PAIRS, 1);
-                wc.add(WC_BYTES, 4);
-            }
+            uint32_t acc[K];
+            const M nm = pull_span<K>(rv, ns, b0, min(rv.col[u + 1], b0 + AXBC_SPAN), fprev, msigma, su, sg,
+                                      acc, wc);
+#pragma unroll
+            for (int h = 0; h < K; h++)
+                if (pbit(nm, h)) {
+                    atomicAdd(&msigma[row_base<K>(u) + 32 * h + lane], acc[h]);
+                    wc.add(WC_PAIRS, 1);
+                    wc.add(WC_BYTES, 4);
+                }
             bool first = false;
-            if (lane == 0 && nm) first = atomicOr(&fcur[u], nm) == 0u;
-            if (lane == 0 && nm) wc.add(WC_BYTES, first ? 8 : 4);  // level mask, list entry
+            if (lane == 0 && nm) first = atomicOr(&fcur[u], nm) == 0;
+            if (lane == 0 && nm) wc.add(WC_BYTES, first ? 4 + 4 * K : 4 * K);  // level mask, list entry
             list_append(ll, L, first, u);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
         for (uint64_t lt = l0; lt < l0 + LIGHT_PER_UNIT && lt < rv.n_ltask; lt++) {
             const uint32_t beg = rv.ltask[lt], cnt = rv.ltask[lt + 1] - beg;
-            uint32_t u_l = 0, ns_l = 0;
+            uint32_t u_l = 0;
+            M ns_l = 0;
             if (lane < cnt) {
                 u_l = rv.order[beg + lane];
                 ns_l = srcmask & ~seen[u_l];
-                wc.add(WC_BYTES, 4);  // seen mask
+                wc.add(WC_BYTES, 4 * K);  // seen mask
             }
-            const uint32_t mine = pull_light32(rv, u_l, ns_l, fprev, msigma, su, sg, sk, wc);
+            const M mine = pull_light32<K>(rv, u_l, ns_l, fprev, msigma, su, sg, sk, wc);
             if (mine) {
                 fcur[u_l] = mine;
-                wc.add(WC_PAIRS, __popc(mine));
-                wc.add(WC_BYTES, 8 + 4 * __popc(mine));  // level mask, list entry, path counts
+                wc.add(WC_PAIRS, __popcll((unsigned long long)mine));
+                wc.add(WC_BYTES, 4 + 4 * K + 4 * __popcll((unsigned long long)mine));  // mask, list, counts
             }
-            list_append(ll, L, mine != 0u, u_l);
+            list_append(ll, L, mine != 0, u_l);
         }
     }
 }
@@ -580,38 +690,42 @@ __device__ __forceinline__ void fwd_pull_body(const Adj &rv, uint32_t srcmask,
 // One forward level, device-driven: the level is bi->cur + 1 and the direction
 // bi->push_next (set by the previous k_level_advance).  Both direction kernels
 // are launched every level; the one not chosen returns at once, as both do
-// once a level discovered nothing.
-// CNT: the counting build (work counts into wc[KP_FWD_PUSH / KP_FWD_PULL]).
-template <bool CNT>
-__global__ void __launch_bounds__(BATCH_TPB, 8) k_fwd_push_step(Adj a, const BatchInfo *__restrict__ bi,
+// once a level discovered nothing.  CNT: the counting build (work counts into
+// wc[KP_FWD_PUSH / KP_FWD_PULL]).
+template <int K, bool CNT>
+__global__ void __launch_bounds__(BATCH_TPB, PUSH_BLOCKS(K)) k_fwd_push_step(Adj a, const BatchInfo *__restrict__ bi,
                                                              uint32_t *const *__restrict__ tab,
                                                              const uint32_t *__restrict__ seen,
                                                              uint32_t *msigma, uint32_t *ctrs,
                                                              LevelLists ll, unsigned long long *wc)
 {
+    typedef typename MaskOf<K>::T M;
     if (!bi->alive || !bi->push_next) return;
     const int L = bi->cur + 1;
     WorkCount<CNT> cnt;
-    fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L, cnt);
+    fwd_push_body<K>(a, reinterpret_cast<const M *>(tab[L - 1]), reinterpret_cast<M *>(tab[L]),
+                     reinterpret_cast<const M *>(seen), msigma, ctrs + 2 * L, ll, L, cnt);
     cnt.flush(wc);
 }
 
-template <bool CNT>
-__global__ void __launch_bounds__(BATCH_TPB, AXBC_PULL_MIN_BLOCKS) k_fwd_pull_step(Adj rv, const BatchInfo *__restrict__ bi,
+template <int K, bool CNT>
+__global__ void __launch_bounds__(BATCH_TPB, PULL_BLOCKS(K)) k_fwd_pull_step(Adj rv, const BatchInfo *__restrict__ bi,
                                                              uint32_t *const *__restrict__ tab,
                                                              const uint32_t *__restrict__ seen,
                                                              uint32_t *msigma, uint32_t *ctrs,
                                                              LevelLists ll, unsigned long long *wc)
 {
+    typedef typename MaskOf<K>::T M;
     __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
-    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_g[BATCH_TPB * K];
     __shared__ uint32_t s_k[BATCH_TPB];
     if (!bi->alive || bi->push_next) return;
     const int L = bi->cur + 1;
     const unsigned w0 = threadIdx.x & ~31u;
     WorkCount<CNT> cnt;
-    fwd_pull_body(rv, bi->srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, s_u + w0, s_g + w0,
-                  s_k + w0, ll, L, cnt);
+    fwd_pull_body<K>(rv, (M)bi->srcmask, reinterpret_cast<const M *>(tab[L - 1]), reinterpret_cast<M *>(tab[L]),
+                     reinterpret_cast<const M *>(seen), msigma, ctrs + 2 * L, s_u + w0, s_g + w0 * K, s_k + w0,
+                     ll, L, cnt);
     cnt.flush(wc);
 }
 
@@ -619,19 +733,19 @@ __global__ void __launch_bounds__(BATCH_TPB, AXBC_PULL_MIN_BLOCKS) k_fwd_pull_st
 // pivot, the vertices reached, their degree sum and their reach sum; subtract
 // from the unvisited-edge total the in-degrees of vertices now seen by every
 // pivot.  Visits only level L's list when stored.
-__device__ __forceinline__ void stats_vertex(uint64_t u, uint32_t srcmask,
-                                             const uint32_t *__restrict__ fcur, uint32_t *seen,
+template <class M>
+__device__ __forceinline__ void stats_vertex(uint64_t u, M srcmask, const M *__restrict__ fcur, M *seen,
                                              const uint32_t *__restrict__ col,
                                              const uint32_t *__restrict__ rcol,
-                                             const uint32_t *__restrict__ reach, uint32_t &nm,
+                                             const uint32_t *__restrict__ reach, M &nm,
                                              uint32_t &d, uint32_t &r, unsigned long long &fdeg,
                                              unsigned long long &udec, bool &any)
 {
     nm = fcur[u];
     if (!nm) return;
     any = true;
-    const uint32_t sn = seen[u];
-    const uint32_t sn2 = sn | nm;
+    const M sn = seen[u];
+    const M sn2 = sn | nm;
     seen[u] = sn2;
     d = col[u + 1] - col[u];
     r = reach[u];
@@ -639,12 +753,14 @@ __device__ __forceinline__ void stats_vertex(uint64_t u, uint32_t srcmask,
     if ((sn & srcmask) != srcmask && (sn2 & srcmask) == srcmask) udec += rcol[u + 1] - rcol[u];
 }
 
-__device__ __forceinline__ void stats_body(uint64_t n, BatchInfo *bi, int L, uint32_t srcmask,
-                                           const uint32_t *__restrict__ fcur, uint32_t *seen,
-                                           const uint32_t *__restrict__ col,
+template <int K>
+__device__ __forceinline__ void stats_body(uint64_t n, BatchInfo *bi, int L, typename MaskOf<K>::T srcmask,
+                                           const typename MaskOf<K>::T *__restrict__ fcur,
+                                           typename MaskOf<K>::T *seen, const uint32_t *__restrict__ col,
                                            const uint32_t *__restrict__ rcol,
                                            const uint32_t *__restrict__ reach, const LevelLists &ll)
 {
+    typedef typename MaskOf<K>::T M;
     const unsigned lane = lane_id();
     const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
@@ -653,33 +769,39 @@ __device__ __forceinline__ void stats_body(uint64_t n, BatchInfo *bi, int L, uin
     const uint64_t items = lst ? lcnt : n;
     const uint64_t nblk = (items + 31) / 32;
     const uint64_t nw = nthreads / 32;
-    unsigned long long cnt = 0, te = 0, rs = 0, fdeg = 0, udec = 0;
+    unsigned long long cnt[K], te[K], rs[K];
+#pragma unroll
+    for (int h = 0; h < K; h++) cnt[h] = te[h] = rs[h] = 0;
+    unsigned long long fdeg = 0, udec = 0, tsum = 0;
     uint32_t hv = 0;  // heavy vertices of the level (their span items are scanned)
     bool any = false;
     for (uint64_t t = tid / 32; t < nblk; t += nw) {
         const uint64_t i = t * 32 + lane;
-        uint32_t nm = 0, d = 0, r = 0;
+        M nm = 0;
+        uint32_t d = 0, r = 0;
         if (i < items) {
             const uint64_t u = lst ? lst[i] : i;
-            stats_vertex(u, srcmask, fcur, seen, col, rcol, reach, nm, d, r, fdeg, udec, any);
+            stats_vertex<M>(u, srcmask, fcur, seen, col, rcol, reach, nm, d, r, fdeg, udec, any);
             if (nm && d > AXBC_SPAN) hv++;
+            tsum += (unsigned long long)d * __popcll((unsigned long long)nm);
         }
         unsigned act = __ballot_sync(FULL_MASK, nm != 0);
         while (act) {
             const int j = __ffs(act) - 1;
             act &= act - 1;
-            const uint32_t mj = __shfl_sync(FULL_MASK, nm, j);
+            const M mj = __shfl_sync(FULL_MASK, nm, j);
             const uint32_t dj = __shfl_sync(FULL_MASK, d, j);
             const uint32_t rj = __shfl_sync(FULL_MASK, r, j);
-            if ((mj >> lane) & 1u) {
-                cnt++;
-                te += dj;
-                rs += rj;
-            }
+#pragma unroll
+            for (int h = 0; h < K; h++)
+                if (pbit(mj, h)) {
+                    cnt[h]++;
+                    te[h] += dj;
+                    rs[h] += rj;
+                }
         }
     }
     {
-        unsigned long long tsum = te;
         uint32_t hsum = hv;
         for (int o = 16; o; o >>= 1) {
             tsum += __shfl_xor_sync(FULL_MASK, tsum, o);
@@ -688,12 +810,15 @@ __device__ __forceinline__ void stats_body(uint64_t n, BatchInfo *bi, int L, uin
         if (lane == 0 && tsum) atomicAdd(&bi->lvl_te, tsum);
         if (lane == 0 && hsum) atomicAdd(&ll.heavy[L], hsum);
     }
-    if (cnt) {
-        atomicAdd(&bi->lvl_new[lane], cnt);
-        atomicAdd(&bi->nvis[lane], cnt);
-        atomicAdd(&bi->te[lane], te);
-        atomicAdd(&bi->rsum[lane], rs);
-    }
+#pragma unroll
+    for (int h = 0; h < K; h++)
+        if (cnt[h]) {
+            const int s = lane + 32 * h;
+            atomicAdd(&bi->lvl_new[s], cnt[h]);
+            atomicAdd(&bi->nvis[s], cnt[h]);
+            atomicAdd(&bi->te[s], te[h]);
+            atomicAdd(&bi->rsum[s], rs[h]);
+        }
     for (int o = 16; o; o >>= 1) {
         fdeg += __shfl_xor_sync(FULL_MASK, fdeg, o);
         udec += __shfl_xor_sync(FULL_MASK, udec, o);
@@ -706,6 +831,7 @@ __device__ __forceinline__ void stats_body(uint64_t n, BatchInfo *bi, int L, uin
     }
 }
 
+template <int K>
 __global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo *bi,
                                                           uint32_t *const *__restrict__ tab,
                                                           uint32_t *seen,
@@ -714,31 +840,39 @@ __global__ void __launch_bounds__(BATCH_TPB) k_stats_step(uint64_t n, BatchInfo 
                                                           const uint32_t *__restrict__ reach,
                                                           LevelLists ll)
 {
+    typedef typename MaskOf<K>::T M;
     if (!bi->alive) return;
     const int L = bi->cur + 1;
-    stats_body(n, bi, L, bi->srcmask, tab[L], seen, col, rcol, reach, ll);
+    stats_body<K>(n, bi, L, (M)bi->srcmask, reinterpret_cast<const M *>(tab[L]), reinterpret_cast<M *>(seen),
+                  col, rcol, reach, ll);
 }
 
-// Close forward level L = bi->cur + 1: per-pivot termination, the per-level
-// totals, the direction of the next level, and -- once nothing was discovered
-// -- the deepest depth and the depth-0 pivots of the backward pass.
-// one warp (lanes = pivots) of the block that closes level L
+// Close forward level L = bi->cur + 1 (one warp, lane l for pivots l + 32 h):
+// per-pivot termination, the per-level totals, the direction of the next
+// level, and -- once nothing was discovered -- the deepest depth and the
+// depth-0 pivots of the backward pass.
+template <int K>
 __device__ __forceinline__ void level_advance_warp(BatchInfo *bi, unsigned long long *level_te,
                                                    unsigned long long *level_cnt, int32_t *level_mode,
                                                    const LevelLists &ll, uint32_t pool_cap,
                                                    uint32_t list_max)
 {
-    const unsigned s = lane_id();
+    const unsigned l = lane_id();
     const int L = bi->cur + 1;
     const uint32_t nsrc = bi->nsrc;
-    const unsigned long long nw = s < nsrc ? bi->lvl_new[s] : 0ull;
-    if (s < nsrc && bi->Ls[s] == 0 && nw == 0) bi->Ls[s] = L;
-    unsigned long long cnt = nw;
+    unsigned long long cnt = 0, d0 = 0;
+#pragma unroll
+    for (int h = 0; h < K; h++) {
+        const uint32_t s = l + 32 * h;
+        const unsigned long long nw = s < nsrc ? bi->lvl_new[s] : 0ull;
+        if (s < nsrc && bi->Ls[s] == 0 && nw == 0) bi->Ls[s] = L;
+        cnt += nw;
+        const bool two = s < nsrc && bi->Ls[s] == 2;
+        d0 |= (unsigned long long)__ballot_sync(FULL_MASK, two) << (32 * h);
+    }
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
-    const bool two = s < nsrc && bi->Ls[s] == 2;
-    const uint32_t d0 = __ballot_sync(FULL_MASK, two);
     __syncwarp();
-    if (s == 0) {
+    if (l == 0) {
         level_te[L] = bi->lvl_te;
         level_cnt[L] = cnt;
         level_mode[L] = bi->push_next;
@@ -766,32 +900,48 @@ __device__ __forceinline__ void level_advance_warp(BatchInfo *bi, unsigned long 
         bi->front_deg = 0;
         bi->any_new = 0;
     }
-    if (s < AXBC_W) bi->lvl_new[s] = 0;
+#pragma unroll
+    for (int h = 0; h < K; h++) bi->lvl_new[l + 32 * h] = 0;
 }
 
+template <int K>
 __global__ void k_level_advance(BatchInfo *bi, unsigned long long *level_te,
                                 unsigned long long *level_cnt, int32_t *level_mode,
                                 LevelLists ll, uint32_t pool_cap, uint32_t list_max)
 {
     if (!bi->alive) return;
-    level_advance_warp(bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max);
+    level_advance_warp<K>(bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max);
 }
 
-// Sum of the 8 staged successor terms of one group as a balanced tree (pairs
-// differing in the lowest position bit first).  mq_l points at lane l of row 0.
-__device__ __forceinline__ float tree8(const uint4 *su4, const uint4 *sg4, int g,
-                                       const float *__restrict__ mq_l, float sv, uint32_t lanebit)
+// The backward pass runs one 32-pivot half of a pass at a time (hh = 0, or 0
+// and 1 for a 64-pivot pass): lane l owns pivot l + 32 hh.  The functions
+// below see the half through offset pointers: level masks as 32-bit words at
+// stride K (word hh of each vertex's mask, little-endian), rows and span
+// partials shifted by 32 hh columns.  A half has the register footprint of a
+// 32-pivot pass, which keeps 8 blocks per SM resident for this latency-bound
+// kernel.
+template <int K> __device__ __forceinline__ uint32_t half_of(typename MaskOf<K>::T m, int hh)
 {
-    const uint4 ua = su4[2 * g], ub = su4[2 * g + 1];
-    const uint4 ga = sg4[2 * g], gb = sg4[2 * g + 1];
-    const uint32_t u[8] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w};
-    const uint32_t m[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
+    return (uint32_t)((unsigned long long)m >> (32 * hh));
+}
+
+// Sum of the 8 staged successor terms of group g as a balanced tree (pairs
+// differing in the lowest position bit first).  mq_l points at the lane's
+// column of row 0.
+template <int K>
+__device__ __forceinline__ float tree8(const uint32_t *su, const uint32_t *sg, int g,
+                                       const float *__restrict__ mq_l, float sv)
+{
+    uint32_t u[8], m[8];
+    load8u(su, g, u);
+    load8u(sg, g, m);
+    const unsigned lane = lane_id();
     float t[8];
 #pragma unroll
     for (int jj = 0; jj < 8; jj++) {
-        const bool h = (m[jj] & lanebit) != 0u;
-        const float q = h ? mq_l[(uint64_t)u[jj] * AXBC_W] : 0.0f;
-        t[jj] = h ? __fmul_rn(q, sv) : 0.0f;
+        const bool hit = (m[jj] >> lane) & 1u;
+        const float q = hit ? mq_l[(uint64_t)u[jj] * (AXBC_W * K)] : 0.0f;
+        t[jj] = hit ? __fmul_rn(q, sv) : 0.0f;
     }
     const float a = __fadd_rn(__fadd_rn(t[0], t[1]), __fadd_rn(t[2], t[3]));
     const float b = __fadd_rn(__fadd_rn(t[4], t[5]), __fadd_rn(t[6], t[7]));
@@ -799,34 +949,30 @@ __device__ __forceinline__ float tree8(const uint4 *su4, const uint4 *sg4, int g
 }
 
 // Canonical dependency sum of vertex v over adjacency positions [b0,b1) for
-// the pivots in f.  q[u][s] = (delta_s[u] + 1) / sigma_s[u] was stored when
-// u's dependency was final, so a successor term is q * sigma_s[v], bit for bit
-// the reference's ((delta + 1) / sigma[r]) * sigma[c].  The 32 positions of a
-// chunk form four 8-position subtrees of the canonical tree; a subtree without
-// successors sums to +0 and is skipped.
-// `un` holds the adjacency entries of the first chunk (row[b0 + lane]).
-template <class WC>
-__device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float sv, uint32_t b0,
-                                               uint32_t b1, uint32_t un, const uint32_t *__restrict__ fnext,
-                                               const float *__restrict__ mq, uint32_t *su, uint32_t *sg,
-                                               WC &wc)
+// the half's pivots in f.  q[u][s] = (delta_s[u] + 1) / sigma_s[u] was stored
+// when u's dependency was final, so a successor term is q * sigma_s[v], bit for
+// bit the reference's ((delta + 1) / sigma[r]) * sigma[c].  The 32 positions
+// of a chunk form four 8-position subtrees of the canonical tree; a subtree
+// without successors sums to +0 and is skipped.  `un` holds the adjacency
+// entries of the first chunk (row[b0 + lane]).
+template <int K, class WC>
+__device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float sv, uint32_t b0, uint32_t b1,
+                                               uint32_t un, const uint32_t *__restrict__ fnext,
+                                               const float *__restrict__ mq, uint32_t *su, uint32_t *sg, WC &wc)
 {
     const unsigned lane = lane_id();
-    const uint32_t lanebit = 1u << lane;
     const float *mq_l = mq + lane;
-    const uint4 *su4 = reinterpret_cast<const uint4 *>(su);
-    const uint4 *sg4 = reinterpret_cast<const uint4 *>(sg);
     float P = 0.0f;
     // the next chunk's adjacency entries load while this chunk is consumed
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t e = base + lane;
         const uint32_t u = un;
         un = e + 32 < b1 ? a.row[e + 32] : 0u;
-        const uint32_t gm = e < b1 ? fnext[u] & f : 0u;
+        const uint32_t gm = e < b1 ? fnext[(uint64_t)u * K] & f : 0u;
         if (e < b1) {
             wc.add(WC_ENTRIES, 1);
             wc.add(WC_GATHERS, __popc(gm));
-            wc.add(WC_BYTES, 8 + 4 * __popc(gm));  // adjacency entry, level mask, successors' q
+            wc.add(WC_BYTES, 8 + 4 * __popc(gm));  // adjacency entry, level mask word, successors' q
         }
         const unsigned pm = __ballot_sync(FULL_MASK, gm != 0);
         if (!pm) continue;
@@ -834,39 +980,40 @@ __device__ __forceinline__ float dep_span_from(const Adj &a, uint32_t f, float s
         sg[lane] = gm;
         __syncwarp();
         float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, g3 = 0.0f;
-        if (pm & 0x000000ffu) g0 = tree8(su4, sg4, 0, mq_l, sv, lanebit);
-        if (pm & 0x0000ff00u) g1 = tree8(su4, sg4, 1, mq_l, sv, lanebit);
-        if (pm & 0x00ff0000u) g2 = tree8(su4, sg4, 2, mq_l, sv, lanebit);
-        if (pm & 0xff000000u) g3 = tree8(su4, sg4, 3, mq_l, sv, lanebit);
+        if (pm & 0x000000ffu) g0 = tree8<K>(su, sg, 0, mq_l, sv);
+        if (pm & 0x0000ff00u) g1 = tree8<K>(su, sg, 1, mq_l, sv);
+        if (pm & 0x00ff0000u) g2 = tree8<K>(su, sg, 2, mq_l, sv);
+        if (pm & 0xff000000u) g3 = tree8<K>(su, sg, 3, mq_l, sv);
         P = __fadd_rn(P, __fadd_rn(__fadd_rn(g0, g1), __fadd_rn(g2, g3)));
         __syncwarp();
     }
     return P;
 }
 
-template <class WC>
-__device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, uint32_t b0,
-                                          uint32_t b1, const uint32_t *__restrict__ fnext,
-                                          const float *__restrict__ mq, uint32_t *su, uint32_t *sg, WC &wc)
+template <int K, class WC>
+__device__ __forceinline__ float dep_span(const Adj &a, uint32_t f, float sv, uint32_t b0, uint32_t b1,
+                                          const uint32_t *__restrict__ fnext, const float *__restrict__ mq,
+                                          uint32_t *su, uint32_t *sg, WC &wc)
 {
     const uint32_t e = b0 + lane_id();
-    return dep_span_from(a, f, sv, b0, b1, e < b1 ? a.row[e] : 0u, fnext, mq, su, sg, wc);
+    return dep_span_from<K>(a, f, sv, b0, b1, e < b1 ? a.row[e] : 0u, fnext, mq, su, sg, wc);
 }
 
-// delta and q of vertex v for the pivots in f
-__device__ __forceinline__ void write_dep(float *mdelta, float *mq, uint32_t v, uint32_t f,
-                                          float delta, uint32_t sig)
+// delta and q of vertex v for the half's pivots in f
+template <int K>
+__device__ __forceinline__ void write_dep(float *mdelta, float *mq, uint32_t v, uint32_t f, float delta,
+                                          uint32_t sig)
 {
     const unsigned lane = lane_id();
     if ((f >> lane) & 1u) {
-        mdelta[row_base(v) + lane] = delta;
-        mq[row_base(v) + lane] = __fdiv_rn(__fadd_rn(delta, 1.0f), __uint2float_rn(sig));
+        mdelta[row_base<K>(v) + lane] = delta;
+        mq[row_base<K>(v) + lane] = __fdiv_rn(__fadd_rn(delta, 1.0f), __uint2float_rn(sig));
     }
 }
 
-// Backward depth d for the pivots in dmask.  With no_succ (the deepest depth)
-// nothing lies below, so delta = reach.
-template <class WC>
+// Backward depth d for the half's pivots in dmask.  With no_succ (the deepest
+// depth) nothing lies below, so delta = reach.
+template <int K, class WC>
 __device__ __forceinline__ void bwd_vertices(const Adj &a, uint32_t v_l, uint32_t f_l, int no_succ,
                                              const uint32_t *__restrict__ fnext,
                                              const uint32_t *__restrict__ msigma, float *mdelta,
@@ -903,19 +1050,18 @@ __device__ __forceinline__ void bwd_vertices(const Adj &a, uint32_t v_l, uint32_
             b1 = __shfl_sync(FULL_MASK, c1_l, jn);
             un = b0 + lane < b1 ? a.row[b0 + lane] : 0u;
         }
-        const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
+        const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base<K>(v) + lane] : 0u;
         float P = 0.0f;
-        if (!no_succ) P = dep_span_from(a, f, __uint2float_rn(sig), cb0, cb1, cu, fnext, mq, su, sg, wc);
-        write_dep(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
+        if (!no_succ) P = dep_span_from<K>(a, f, __uint2float_rn(sig), cb0, cb1, cu, fnext, mq, su, sg, wc);
+        write_dep<K>(mdelta, mq, v, f, __fadd_rn(__uint2float_rn(reach[v]), P), sig);
         if (jn < 0) break;
         j = jn;
     }
 }
 
-template <class WC>
+template <int K, class WC>
 __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_succ,
-                                         const uint32_t *__restrict__ fd,
-                                         const uint32_t *__restrict__ fnext,
+                                         const uint32_t *__restrict__ fd, const uint32_t *__restrict__ fnext,
                                          const uint32_t *__restrict__ msigma, float *mdelta,
                                          float *mq, float *mpartial,
                                          const uint32_t *__restrict__ reach, uint32_t *ctr,
@@ -933,16 +1079,17 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
         if (t >= nu) break;
         if (t < nhi) {
             const uint32_t v = a.hitem_v[t];
-            const uint32_t f = fd[v] & dmask;
-            if (lane == 0) wc.add(WC_BYTES, 4);  // level mask
+            const uint32_t f = fd[(uint64_t)v * K] & dmask;
+            if (lane == 0) wc.add(WC_BYTES, 4);  // level mask word
             if (!f) continue;
             float P = 0.0f;
             if (!no_succ) {
-                const float sv = __uint2float_rn(((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u);
+                const float sv =
+                    __uint2float_rn(((f >> lane) & 1u) ? msigma[row_base<K>(v) + lane] : 0u);
                 const uint32_t b0 = a.col[v] + a.hitem_k[t] * AXBC_SPAN;
-                P = dep_span(a, f, sv, b0, min(a.col[v + 1], b0 + AXBC_SPAN), fnext, mq, su, sg, wc);
+                P = dep_span<K>(a, f, sv, b0, min(a.col[v + 1], b0 + AXBC_SPAN), fnext, mq, su, sg, wc);
             }
-            mpartial[(uint64_t)t * AXBC_W + lane] = P;
+            mpartial[(uint64_t)t * (AXBC_W * K) + lane] = P;
             if ((f >> lane) & 1u) wc.add(WC_BYTES, 8);  // path count read, span partial written
             continue;
         }
@@ -951,10 +1098,10 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
             uint32_t v_l = 0, f_l = 0;
             if (lane < ent && i < lcnt) {
                 v_l = lst[i];
-                if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fd[v_l] & dmask;
-                wc.add(WC_BYTES, 8);  // list entry, level mask
+                if (a.col[v_l + 1] - a.col[v_l] <= AXBC_SPAN) f_l = fd[(uint64_t)v_l * K] & dmask;
+                wc.add(WC_BYTES, 8);  // list entry, level mask word
             }
-            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg, wc);
+            bwd_vertices<K>(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg, wc);
             continue;
         }
         const uint64_t l0 = (uint64_t)(t - nhi) * LIGHT_PER_UNIT;
@@ -963,17 +1110,19 @@ __device__ __forceinline__ void bwd_body(const Adj &a, uint32_t dmask, int no_su
             uint32_t v_l = 0, f_l = 0;
             if (lane < cnt) {
                 v_l = a.order[beg + lane];
-                f_l = fd[v_l] & dmask;
-                wc.add(WC_BYTES, 4);  // level mask
+                f_l = fd[(uint64_t)v_l * K] & dmask;
+                wc.add(WC_BYTES, 4);  // level mask word
             }
-            bwd_vertices(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg, wc);
+            bwd_vertices<K>(a, v_l, f_l, no_succ, fnext, msigma, mdelta, mq, reach, su, sg, wc);
         }
     }
 }
 
-// One backward depth, device-driven: d = bi->bd (a no-op once below 0).
-// CNT: the counting build (work counts into wc[KP_BWD]).
-template <bool CNT>
+// One backward depth, device-driven: d = bi->bd (a no-op once below 0).  The
+// grid's y index is the half: the blocks of half 1 of a 64-pivot pass start as
+// those of half 0 run out of work, each half with its own work counter.  CNT:
+// the counting build (work counts into wc[KP_BWD]).
+template <int K, bool CNT>
 __global__ void __launch_bounds__(BATCH_TPB, AXBC_BWD_MIN_BLOCKS) k_bwd_step(Adj a, const BatchInfo *__restrict__ bi,
                                                         uint32_t *const *__restrict__ tab,
                                                         const uint32_t *__restrict__ msigma,
@@ -982,23 +1131,26 @@ __global__ void __launch_bounds__(BATCH_TPB, AXBC_BWD_MIN_BLOCKS) k_bwd_step(Adj
                                                         uint32_t *ctrs, LevelLists ll,
                                                         unsigned long long *wc)
 {
+    typedef typename MaskOf<K>::T M;
     __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
     __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
     const int d = bi->bd;
     if (d < 0) return;
-    const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
+    const int hh = K == 1 ? 0 : blockIdx.y;
+    const uint32_t dmask = half_of<K>((M)(d >= 1 ? bi->srcmask : bi->depth0mask), hh);
     if (!dmask) return;
     uint32_t *su = s_u + (threadIdx.x & ~31u), *sg = s_g + (threadIdx.x & ~31u);
     uint32_t lcnt = 0;
     const uint32_t *lst = level_list(ll, d, lcnt);
     WorkCount<CNT> cnt;
-    bwd_body(a, dmask, d == bi->dmax, tab[d], tab[d + 1], msigma, mdelta, mq, mpartial, reach,
-             ctrs + 2 * d + 1, su, sg, lst, lcnt, ll.heavy[d], cnt);
+    bwd_body<K>(a, dmask, d == bi->dmax, tab[d] + hh, tab[d + 1] + hh, msigma + 32 * hh, mdelta + 32 * hh,
+                mq + 32 * hh, mpartial + 32 * hh, reach, ctrs + 2 * AXBC_MAX_LEVELS * hh + 2 * d + 1, su, sg, lst,
+                lcnt, ll.heavy[d], cnt);
     cnt.flush(wc);
 }
 
-__device__ __forceinline__ void combine_body(const Adj &a, uint32_t dmask,
-                                             const uint32_t *__restrict__ fd,
+template <int K>
+__device__ __forceinline__ void combine_body(const Adj &a, uint32_t dmask, const uint32_t *__restrict__ fd,
                                              const uint32_t *__restrict__ msigma, float *mdelta,
                                              float *mq, const float *__restrict__ mpartial,
                                              const uint32_t *__restrict__ reach)
@@ -1007,36 +1159,39 @@ __device__ __forceinline__ void combine_body(const Adj &a, uint32_t dmask,
     const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
     for (uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; i < a.n_heavy; i += nw) {
         const uint32_t v = a.heavy_v[i];
-        const uint32_t f = fd[v] & dmask;
+        const uint32_t f = fd[(uint64_t)v * K] & dmask;
         if (!f) continue;
         float acc = __uint2float_rn(reach[v]);
         for (uint32_t k = a.heavy_first[i]; k < a.heavy_first[i + 1]; k++)
-            acc = __fadd_rn(acc, mpartial[(uint64_t)k * AXBC_W + lane]);
-        const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base(v) + lane] : 0u;
-        write_dep(mdelta, mq, v, f, acc, sig);
+            acc = __fadd_rn(acc, mpartial[(uint64_t)k * (AXBC_W * K) + lane]);
+        const uint32_t sig = ((f >> lane) & 1u) ? msigma[row_base<K>(v) + lane] : 0u;
+        write_dep<K>(mdelta, mq, v, f, acc, sig);
     }
 }
 
+template <int K>
 __global__ void k_bwd_combine_step(Adj a, const BatchInfo *__restrict__ bi,
                                    uint32_t *const *__restrict__ tab,
                                    const uint32_t *__restrict__ msigma, float *mdelta, float *mq,
                                    const float *__restrict__ mpartial,
                                    const uint32_t *__restrict__ reach, LevelLists ll)
 {
+    typedef typename MaskOf<K>::T M;
     const int d = bi->bd;
     if (d < 0) return;
     uint32_t lcnt;
     if (level_list(ll, d, lcnt) && ll.heavy[d] == 0) return;  // no heavy vertex at this depth
-    const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
+    const int hh = K == 1 ? 0 : blockIdx.y;
+    const uint32_t dmask = half_of<K>((M)(d >= 1 ? bi->srcmask : bi->depth0mask), hh);
     if (!dmask) return;
-    combine_body(a, dmask, tab[d], msigma, mdelta, mq, mpartial, reach);
+    combine_body<K>(a, dmask, tab[d] + hh, msigma + 32 * hh, mdelta + 32 * hh, mq + 32 * hh, mpartial + 32 * hh,
+                    reach);
 }
 
 __global__ void k_bwd_advance(BatchInfo *bi)
 {
     if (bi->bd >= 0) bi->bd--;
 }
-
 // ------------------------------------------------ persistent level loop
 // On graphs of many narrow levels (grids, roads) a level's work is a few
 // microseconds and the four launches per forward level and three per
@@ -1105,7 +1260,7 @@ __device__ __forceinline__ bool grid_barrier(GridSync *gs, long long budget, int
     return role >= 0;
 }
 
-struct AdvanceLead {
+template <int K> struct AdvanceLead {
     BatchInfo *bi;
     unsigned long long *level_te, *level_cnt;
     int32_t *level_mode;
@@ -1113,7 +1268,7 @@ struct AdvanceLead {
     uint32_t pool_cap, list_max;
     __device__ void operator()() const
     {
-        level_advance_warp(bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max);
+        level_advance_warp<K>(bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max);
     }
 };
 struct BwdLead {
@@ -1129,18 +1284,21 @@ struct BwdLead {
 // phases of the one launch.  Levels stop at lmax (the masks allocated): the
 // kernel sets gs->need and the host grows the tables and launches again, the
 // loop resuming from the level state in bi.
+template <int K>
 __global__ void __launch_bounds__(BATCH_TPB) k_traverse_persist(
-    Adj a, Adj rv, BatchInfo *bi, uint32_t **tab, uint32_t *seen, uint32_t *msigma, float *mdelta,
+    Adj a, Adj rv, BatchInfo *bi, uint32_t **tab, uint32_t *seen_, uint32_t *msigma, float *mdelta,
     float *mq, float *mpartial, const uint32_t *reach, uint32_t *ctrs, LevelLists ll,
     unsigned long long *level_te, unsigned long long *level_cnt, int32_t *level_mode,
     uint32_t pool_cap, uint32_t list_max, uint64_t n, int lmax, GridSync *gs, long long budget)
 {
+    typedef typename MaskOf<K>::T M;
     __shared__ __align__(16) uint32_t s_u[BATCH_TPB];
-    __shared__ __align__(16) uint32_t s_g[BATCH_TPB];
+    __shared__ __align__(16) uint32_t s_g[BATCH_TPB * K];
     __shared__ uint32_t s_k[BATCH_TPB];
     const unsigned w0 = threadIdx.x & ~31u;
+    M *seen = reinterpret_cast<M *>(seen_);
     WorkCount<false> none;
-    const AdvanceLead adv{bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max};
+    const AdvanceLead<K> adv{bi, level_te, level_cnt, level_mode, ll, pool_cap, list_max};
     for (;;) {
         if (!vload_i(&bi->alive)) break;
         const int L = vload_i(&bi->cur) + 1;
@@ -1148,30 +1306,42 @@ __global__ void __launch_bounds__(BATCH_TPB) k_traverse_persist(
             if (blockIdx.x == 0 && threadIdx.x == 0) gs->need = 1;
             return;
         }
-        const uint32_t srcmask = bi->srcmask;
+        const M srcmask = (M)bi->srcmask;
+        M *fprev = reinterpret_cast<M *>(tab[L - 1]), *fcur = reinterpret_cast<M *>(tab[L]);
         if (vload_i(&bi->push_next))
-            fwd_push_body(a, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, ll, L, none);
+            fwd_push_body<K>(a, fprev, fcur, seen, msigma, ctrs + 2 * L, ll, L, none);
         else
-            fwd_pull_body(rv, srcmask, tab[L - 1], tab[L], seen, msigma, ctrs + 2 * L, s_u + w0, s_g + w0,
-                          s_k + w0, ll, L, none);
+            fwd_pull_body<K>(rv, srcmask, fprev, fcur, seen, msigma, ctrs + 2 * L, s_u + w0, s_g + w0 * K,
+                             s_k + w0, ll, L, none);
         if (!grid_barrier(gs, budget, 1, NoLead{})) return;
-        stats_body(n, bi, L, srcmask, tab[L], seen, a.col, rv.col, reach, ll);
+        stats_body<K>(n, bi, L, srcmask, fcur, seen, a.col, rv.col, reach, ll);
         if (!grid_barrier(gs, budget, 2, adv)) return;
     }
     const BwdLead down{bi};
     for (;;) {
         const int d = vload_i(&bi->bd);
         if (d < 0) break;
-        const uint32_t dmask = d >= 1 ? bi->srcmask : bi->depth0mask;
+        const M dmask = (M)(d >= 1 ? bi->srcmask : bi->depth0mask);
         if (dmask) {
             uint32_t lcnt = 0;
             const uint32_t *lst = level_list(ll, d, lcnt);
             const uint32_t lheavy = ll.heavy[d];
-            bwd_body(a, dmask, d == bi->dmax, tab[d], tab[d + 1], msigma, mdelta, mq, mpartial, reach,
-                     ctrs + 2 * d + 1, s_u + w0, s_g + w0, lst, lcnt, lheavy, none);
+            // the halves touch disjoint columns and have their own work
+            // counters: one phase takes both
+        #pragma unroll 1
+    for (int hh = 0; hh < K; hh++)
+                if (half_of<K>(dmask, hh))
+                    bwd_body<K>(a, half_of<K>(dmask, hh), d == bi->dmax, tab[d] + hh, tab[d + 1] + hh,
+                                msigma + 32 * hh, mdelta + 32 * hh, mq + 32 * hh, mpartial + 32 * hh, reach,
+                                ctrs + 2 * AXBC_MAX_LEVELS * hh + 2 * d + 1, s_u + w0, s_g + w0, lst, lcnt, lheavy,
+                                none);
             if (a.n_heavy && !(lst && lheavy == 0)) {
                 if (!grid_barrier(gs, budget, 3, NoLead{})) return;
-                combine_body(a, dmask, tab[d], msigma, mdelta, mq, mpartial, reach);
+            #pragma unroll 1
+    for (int hh = 0; hh < K; hh++)
+                    if (half_of<K>(dmask, hh))
+                        combine_body<K>(a, half_of<K>(dmask, hh), tab[d] + hh, msigma + 32 * hh, mdelta + 32 * hh,
+                                        mq + 32 * hh, mpartial + 32 * hh, reach);
             }
         }
         if (!grid_barrier(gs, budget, 4, down)) return;
@@ -1200,7 +1370,7 @@ __global__ void __launch_bounds__(BATCH_TPB) k_barrier_selftest(GridSync *gs, in
 // bc update for the applied pivots in lane order (update_bc, src/cuda_kernels.cu:
 // 269-286), each into its lane's bc vector.  A pivot that did not reach v
 // contributes delta = reach[v].  Zero terms are skipped: x + float(0/p) == x for
-// p > 0.  One thread per vertex, its 32 dependencies read from rows a warp
+// p > 0.  One thread per vertex, its 32 K dependencies read from rows a warp
 // staged in shared memory.
 // 4-byte global -> shared copies that bypass registers (cp.async), so a warp
 // keeps up to 32 row loads of one chunk and the next chunk's in flight
@@ -1216,43 +1386,52 @@ template <int N> __device__ __forceinline__ void cp_async_wait()
 }
 
 // stage the dependency rows of the chunk's reached vertices: lane l copies
-// column l of each row
-__device__ __forceinline__ void stage_rows(float (*rows)[33], const float *__restrict__ mdelta,
-                                           uint64_t base, uint32_t sv)
+// columns l + 32 h of each row
+template <int K, class M>
+__device__ __forceinline__ void stage_rows(float (*rows)[AXBC_W * K + 1], const float *__restrict__ mdelta,
+                                           uint64_t base, M sv)
 {
     const unsigned lane = lane_id();
-    unsigned need = __ballot_sync(FULL_MASK, sv != 0u);
+    unsigned need = __ballot_sync(FULL_MASK, sv != 0);
     while (need) {
         const int r = __ffs(need) - 1;
         need &= need - 1;
-        cp_async4(&rows[r][lane], mdelta + row_base(base + r) + lane);
+#pragma unroll
+        for (int h = 0; h < K; h++)
+            cp_async4(&rows[r][32 * h + lane], mdelta + row_base<K>(base + r) + 32 * h + lane);
     }
     cp_async_commit();
 }
 
-#define UPD_TPB 128  // 34 KB of staged rows per block
-__global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ mdelta,
-                                                      const uint32_t *__restrict__ seen,
-                                                      const uint32_t *__restrict__ reach, uint64_t n,
-                                                      const BatchInfo *__restrict__ bi,
-                                                      float *__restrict__ delta_out)
+// threads of the update: 128 (34 KB of staged rows) for 32 pivots, 64 for 64
+#define UPD_TPB(K) (128 / (K))
+template <int K>
+__global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict__ mdelta,
+                                                         const uint32_t *__restrict__ seen_,
+                                                         const uint32_t *__restrict__ reach, uint64_t n,
+                                                         const BatchInfo *__restrict__ bi,
+                                                         float *__restrict__ delta_out)
 {
-    __shared__ uint32_t s_root[AXBC_W], s_reach[AXBC_W], s_skip0[AXBC_W];
-    __shared__ double s_p[AXBC_W];
-    __shared__ unsigned long long s_nvt[AXBC_W];
-    __shared__ InvSplit s_iv[AXBC_W];
-    __shared__ float *s_bc[AXBC_W];
+    typedef typename MaskOf<K>::T M;
+    constexpr int NS = AXBC_W * K;  // pivot slots
+    constexpr int TPB = UPD_TPB(K);
+    const M *seen = reinterpret_cast<const M *>(seen_);
+    __shared__ uint32_t s_root[NS], s_reach[NS], s_skip0[NS];
+    __shared__ double s_p[NS];
+    __shared__ unsigned long long s_nvt[NS];
+    __shared__ InvSplit s_iv[NS];
+    __shared__ float *s_bc[NS];
     // per lane: float(reach_v0 + 1), the split 1/p, and whether the fast
     // division applies (bit 0) and zero terms may be skipped (bit 1)
-    __shared__ float4 s_k[AXBC_W];
+    __shared__ float4 s_k[NS];
     __shared__ int s_single;  // every applied lane updates the same vector
     __shared__ int s_allpos;  // every applied lane has p > 0 (zero terms vanish)
-    // per warp, two chunks: the dependency rows of 32 vertices, padded to 33
-    // floats so that thread t reading row t, column s hits bank (t + s) mod 32
-    __shared__ float s_rows[UPD_TPB / 32][2][32][33];
-    const uint32_t amask = bi->applymask & bi->srcmask;
-    if (threadIdx.x < AXBC_W) {
-        const int s = threadIdx.x;
+    // per warp, two chunks: the dependency rows of 32 vertices, padded to
+    // NS + 1 floats so that thread t reading row t, column s hits bank
+    // (t + s) mod 32
+    __shared__ float s_rows[TPB / 32][2][32][NS + 1];
+    const M amask = (M)(bi->applymask & bi->srcmask);
+    for (int s = threadIdx.x; s < NS; s += TPB) {
         s_bc[s] = bi->lane_bc[s];
         if ((amask >> s) & 1u) {
             const uint32_t r = bi->root[s];
@@ -1278,7 +1457,7 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         if (s == 0) {
             int single = 1, allpos = 1;
             float *t0 = nullptr;
-            for (int l = 0; l < AXBC_W; l++)
+            for (int l = 0; l < NS; l++)
                 if ((amask >> l) & 1u) {
                     if (!t0) t0 = bi->lane_bc[l];
                     else if (bi->lane_bc[l] != t0) single = 0;
@@ -1294,32 +1473,34 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
     // a vertex no pivot reached, with reach 0, gets only zero terms: skipped
     // when they vanish (p > 0; 0/0 is NaN, as in the reference)
     const bool skip_unreached = s_allpos != 0;
-    const int slast = 31 - __clz(amask);
+    const int slast = 63 - __clzll((unsigned long long)amask);
     // delta_out (when given): the last applied pivot's dependencies, taken
     // from the staged rows (k_extract_delta's rule)
     const uint32_t dl_root = bi->root[slast];
     const bool dl_root_done = (bi->depth0mask >> slast) & 1u;
     const unsigned lane = lane_id();
     const unsigned wid = threadIdx.x >> 5;
-    const uint64_t stride = (uint64_t)gridDim.x * (UPD_TPB / 32) * 32;
-    uint64_t base = (blockIdx.x * (uint64_t)(UPD_TPB / 32) + wid) * 32;
+    const uint64_t stride = (uint64_t)gridDim.x * (TPB / 32) * 32;
+    uint64_t base = (blockIdx.x * (uint64_t)(TPB / 32) + wid) * 32;
     if (base >= n) return;
-    uint32_t sv = 0, rv = 0;
+    M sv = 0;
+    uint32_t rv = 0;
     if (base + lane < n) {
         sv = seen[base + lane];
         rv = reach[base + lane];
     }
-    stage_rows(s_rows[wid][0], mdelta, base, sv);
+    stage_rows<K>(s_rows[wid][0], mdelta, base, sv);
     for (int buf = 0; base < n; base += stride, buf ^= 1) {
         // the next chunk's rows load while this chunk is summed
         const uint64_t next = base + stride;
-        uint32_t svn = 0, rvn = 0;
+        M svn = 0;
+        uint32_t rvn = 0;
         if (next + lane < n) {
             svn = seen[next + lane];
             rvn = reach[next + lane];
         }
         if (next < n) {
-            stage_rows(s_rows[wid][buf ^ 1], mdelta, next, svn);
+            stage_rows<K>(s_rows[wid][buf ^ 1], mdelta, next, svn);
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
@@ -1332,16 +1513,16 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
         }
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
-        const bool work = v < n && (sv != 0u || rv != 0u || !skip_unreached);
+        const bool work = v < n && (sv != 0 || rv != 0u || !skip_unreached);
         if (work && single && rv == 0u && skip_unreached) {
             // one target vector, reach 0, every p > 0: a pivot that did not
             // reach v adds +0, so only the reached lanes are visited, in lane
             // order (roots are reached by their own lane)
-            const float(*rows)[33] = s_rows[wid][buf];
+            const float(*rows)[NS + 1] = s_rows[wid][buf];
             float *tgt = s_bc[slast];
             float b = tgt[v];
-            for (uint32_t bits = sv & amask; bits; bits &= bits - 1u) {
-                const int s = __ffs(bits) - 1;
+            for (M bits = sv & amask; bits; bits &= bits - 1) {
+                const int s = __ffsll((unsigned long long)bits) - 1;
                 if ((uint32_t)v == s_root[s]) {
                     if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
                     continue;
@@ -1354,13 +1535,13 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
             }
             tgt[v] = b;
         } else if (work && single) {
-            // one target vector: all 32 lanes unrolled, lane order kept
-            const float(*rows)[33] = s_rows[wid][buf];
+            // one target vector: every slot in order
+            const float(*rows)[NS + 1] = s_rows[wid][buf];
             const float rf = __uint2float_rn(rv);
             float *tgt = s_bc[slast];
             float b = tgt[v];
 #pragma unroll
-            for (int s = 0; s < AXBC_W; s++) {
+            for (int s = 0; s < NS; s++) {
                 if (!((amask >> s) & 1u)) continue;
                 if ((uint32_t)v == s_root[s]) {
                     if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
@@ -1374,7 +1555,7 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
             }
             tgt[v] = b;
         } else if (work) {
-            const float(*rows)[33] = s_rows[wid][buf];
+            const float(*rows)[NS + 1] = s_rows[wid][buf];
             const float rf = __uint2float_rn(rv);
             // lanes in order; consecutive lanes of one run add into one
             // register, written back when the target vector changes
@@ -1404,47 +1585,53 @@ __global__ void __launch_bounds__(UPD_TPB) k_update_m(const float *__restrict__ 
 }
 
 // the last applied pivot's dependencies as a plain n-vector
+template <int K>
 __global__ void k_extract_delta(float *out, const float *__restrict__ mdelta,
-                                const uint32_t *__restrict__ seen,
+                                const uint32_t *__restrict__ seen_,
                                 const uint32_t *__restrict__ reach, uint64_t n,
                                 const BatchInfo *__restrict__ bi, int lane_lo, int lane_hi)
 {
+    typedef typename MaskOf<K>::T M;
+    const M *seen = reinterpret_cast<const M *>(seen_);
     // the highest applied lane of [lane_lo, lane_hi)
-    uint32_t range = lane_hi >= 32 ? FULL_MASK : ((1u << lane_hi) - 1u);
-    range &= ~((1u << lane_lo) - 1u);
-    const uint32_t am = bi->applymask & bi->srcmask & range;
+    unsigned long long range = lane_hi >= 64 ? ~0ull : ((1ull << lane_hi) - 1ull);
+    range &= ~((1ull << lane_lo) - 1ull);
+    const unsigned long long am = bi->applymask & bi->srcmask & range;
     if (am == 0) return;
-    const int s = 31 - __clz(am);
+    const int s = 63 - __clzll(am);
     const uint32_t root = bi->root[s];
-    const bool root_done = (bi->depth0mask >> s) & 1u;
+    const bool root_done = (bi->depth0mask >> s) & 1ull;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
          v += (uint64_t)gridDim.x * blockDim.x) {
-        bool have = (seen[v] >> s) & 1u;
+        bool have = ((unsigned long long)seen[v] >> s) & 1ull;
         if (v == root) have = root_done;
-        out[v] = have ? mdelta[row_base(v) + s] : __uint2float_rn(reach[v]);
+        out[v] = have ? mdelta[row_base<K>(v) + s] : __uint2float_rn(reach[v]);
     }
 }
 
 // one pivot of the last batch: path counts, depths, dependencies
-__global__ void k_source_view(int s, int levels, uint32_t *const *fm, const uint32_t *__restrict__ seen,
+template <int K>
+__global__ void k_source_view(int s, int levels, uint32_t *const *fm, const uint32_t *__restrict__ seen_,
                               const uint32_t *__restrict__ msigma, const float *__restrict__ mdelta,
-                              const uint32_t *__restrict__ reach, uint64_t n, uint32_t depth0,
+                              const uint32_t *__restrict__ reach, uint64_t n, unsigned long long depth0,
                               uint32_t *sig, int32_t *lvl, float *dl)
 {
+    typedef typename MaskOf<K>::T M;
+    const M *seen = reinterpret_cast<const M *>(seen_);
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
          v += (uint64_t)gridDim.x * blockDim.x) {
         int L = -1;
-        if ((seen[v] >> s) & 1u) {
+        if (((unsigned long long)seen[v] >> s) & 1ull) {
             for (int l = 0; l < levels; l++)
-                if ((fm[l][v] >> s) & 1u) {
+                if (((unsigned long long)reinterpret_cast<const M *>(fm[l])[v] >> s) & 1ull) {
                     L = l;
                     break;
                 }
         }
         lvl[v] = L;
-        sig[v] = L >= 0 ? msigma[row_base(v) + s] : 0u;
-        bool have = L > 0 || (L == 0 && ((depth0 >> s) & 1u));
-        dl[v] = have ? mdelta[row_base(v) + s] : __uint2float_rn(reach[v]);
+        sig[v] = L >= 0 ? msigma[row_base<K>(v) + s] : 0u;
+        bool have = L > 0 || (L == 0 && ((depth0 >> s) & 1ull));
+        dl[v] = have ? mdelta[row_base<K>(v) + s] : __uint2float_rn(reach[v]);
     }
 }
 
@@ -1452,13 +1639,14 @@ static int ensure_level_tables(axbc_ctx *c)
 {
     if (c->tables_ready) return AXBC_OK;
     ALLOC_MISSING(c->fmtab, AXBC_MAX_LEVELS * sizeof(uint32_t *), &c->bytes);
-    ALLOC_MISSING(c->ctrs, 2 * AXBC_MAX_LEVELS * 4, &c->bytes);
+    ALLOC_MISSING(c->ctrs, 2 * AXBC_WMAX / 32 * AXBC_MAX_LEVELS * 4, &c->bytes);
     ALLOC_MISSING(c->d_level_te, AXBC_MAX_LEVELS * 8, &c->bytes);
     ALLOC_MISSING(c->d_level_cnt, AXBC_MAX_LEVELS * 8, &c->bytes);
     ALLOC_MISSING(c->d_level_mode, AXBC_MAX_LEVELS * 4, &c->bytes);
     // level lists: a vertex joins a level's list once per distinct depth at
-    // which the batch's pivots reach it, so 32 n entries never run out; a
-    // level may hold up to n/8 vertices before it falls back to the task scan
+    // which the batch's pivots reach it (at most 64 n entries); the pool
+    // starts at 32 n and grows when a batch runs short; a level may hold up to
+    // n/8 vertices before it falls back to the task scan
     if (!c->lpool) {
         const uint32_t cap = (uint32_t)std::min<uint64_t>((uint64_t)AXBC_W * c->g->n + 64, 0xffffffffull);
         TRY(axbc_dalloc((void **)&c->lpool, (uint64_t)cap * 4, &c->bytes));
@@ -1486,7 +1674,9 @@ static uint32_t list_max_of(const axbc_ctx *c)
     return (uint32_t)std::max<uint64_t>(64, c->g->max_deg <= 64 ? n / 2 : n / 8);
 }
 
-// Level masks 0..levels-1 exist, and their pointers are in the device table.
+// Level masks 0..levels-1 exist (two words per vertex, enough for either
+// width), and their pointers are in the device table.  Every mask array is
+// all zero between batches.
 int axbc_batch_levels_alloc(axbc_ctx *c, int levels)
 {
     TRY(ensure_level_tables(c));
@@ -1499,9 +1689,9 @@ int axbc_batch_levels_alloc(axbc_ctx *c, int levels)
     int rc = AXBC_OK;
     while ((int)c->fmask.size() < levels) {
         uint32_t *p = nullptr;
-        if ((rc = axbc_dalloc((void **)&p, c->g->n * 4, &c->bytes)) != AXBC_OK) break;
+        if ((rc = axbc_dalloc((void **)&p, c->g->n * 8, &c->bytes)) != AXBC_OK) break;
         c->fmask.push_back(p);
-        CU(cudaMemset(p, 0, c->g->n * 4));
+        CU(cudaMemset(p, 0, c->g->n * 8));
     }
     if (c->fmask.size() > c->fmtab_synced) {
         CU(cudaMemcpy(c->fmtab + c->fmtab_synced, c->fmask.data() + c->fmtab_synced,
@@ -1511,92 +1701,98 @@ int axbc_batch_levels_alloc(axbc_ctx *c, int levels)
     return rc;
 }
 
+// per-pivot rows of 64 values, masks of two words: a pass of either width
 int axbc_ensure_batch(axbc_ctx *c)
 {
     if (c->batch_ready) return AXBC_OK;
     const uint64_t n = c->g->n;
-    ALLOC_MISSING(c->seen, n * 4, &c->bytes);
-    ALLOC_MISSING(c->msigma, n * AXBC_W * 4, &c->bytes);
-    ALLOC_MISSING(c->mdelta, n * AXBC_W * 4, &c->bytes);
-    ALLOC_MISSING(c->mq, n * AXBC_W * 4, &c->bytes);
+    ALLOC_MISSING(c->seen, n * 8, &c->bytes);
+    ALLOC_MISSING(c->msigma, n * AXBC_WMAX * 4, &c->bytes);
+    ALLOC_MISSING(c->mdelta, n * AXBC_WMAX * 4, &c->bytes);
+    ALLOC_MISSING(c->mq, n * AXBC_WMAX * 4, &c->bytes);
     ALLOC_MISSING(c->task_ctr, 64, &c->bytes);
-    ALLOC_MISSING(c->mpartial, (c->g->fwd.n_heavy_items + 1) * AXBC_W * 4, &c->bytes);
+    ALLOC_MISSING(c->mpartial, (c->g->fwd.n_heavy_items + 1) * AXBC_WMAX * 4, &c->bytes);
     ALLOC_MISSING(c->bi, sizeof(BatchInfo), &c->bytes);
     if (!c->bi_host) CU(cudaMallocHost((void **)&c->bi_host, sizeof(BatchInfo)));
     CU(cudaMemset(c->bi, 0, sizeof(BatchInfo)));
+    CU(cudaMemset(c->seen, 0, n * 8));
     TRY(axbc_batch_levels_alloc(c, 10));
     c->batch_ready = true;
     return AXBC_OK;
 }
 
-static int dyn_grid(axbc_ctx *c)
+// mask words per vertex for a pass of nsrc pivots
+static int width_k(int nsrc) { return nsrc > AXBC_W ? 2 : 1; }
+
+// dynamic kernels: as many blocks as stay resident; work comes from counters
+template <int K> static int occupancy(axbc_ctx *c)
 {
-    // dynamic kernels: as many blocks as stay resident; work comes from counters
-    if (!c->dyn_blocks_per_sm) {
+    const int i = K - 1;
+    if (!c->dyn_blocks_per_sm[i]) {
         int a = 0, b = 0, d = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_step<false>, BATCH_TPB, 0));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step<false>, BATCH_TPB, 0));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_fwd_pull_step<false>, BATCH_TPB, 0));
-        c->dyn_blocks_per_sm = std::max(1, a);
-        c->pull_blocks_per_sm = std::max(1, d);
-        c->bwd_blocks_per_sm = std::max(1, b);
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fwd_push_step<K, false>, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bwd_step<K, false>, BATCH_TPB, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_fwd_pull_step<K, false>, BATCH_TPB, 0));
+        c->dyn_blocks_per_sm[i] = std::max(1, a);
+        c->pull_blocks_per_sm[i] = std::max(1, d);
+        c->bwd_blocks_per_sm[i] = std::max(1, b);
     }
-    return axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm);
+    return AXBC_OK;
 }
-
-static int bwd_grid(axbc_ctx *c)
-{
-    dyn_grid(c);
-    return axbc_grid_for(c, BATCH_TPB, c->bwd_blocks_per_sm);
-}
-
-static int pull_grid(axbc_ctx *c)
-{
-    dyn_grid(c);
-    return axbc_grid_for(c, BATCH_TPB, c->pull_blocks_per_sm);
-}
+template <int K> static int push_grid(axbc_ctx *c) { return axbc_grid_for(c, BATCH_TPB, c->dyn_blocks_per_sm[K - 1]); }
+template <int K> static int pull_grid(axbc_ctx *c) { return axbc_grid_for(c, BATCH_TPB, c->pull_blocks_per_sm[K - 1]); }
+template <int K> static int bwd_grid(axbc_ctx *c) { return axbc_grid_for(c, BATCH_TPB, c->bwd_blocks_per_sm[K - 1]); }
 
 // the kernels of one forward level / one backward depth, in stream order
-static void fwd_step_kernels(axbc_ctx *c, int dgrid, int sgrid)
+template <int K> static void fwd_step_kernels(axbc_ctx *c, int sgrid)
 {
     axbc_graph *g = c->g;
     const LevelLists ll = lists_of(c);
-    k_fwd_push_step<false><<<dgrid, BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->seen, c->msigma,
-                                                               c->ctrs, ll, nullptr);
-    k_fwd_pull_step<false><<<pull_grid(c), BATCH_TPB, 0, c->stream>>>(g->rev, c->bi, c->fmtab, c->seen,
-                                                                      c->msigma, c->ctrs, ll, nullptr);
-    k_stats_step<<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->fwd.col,
-                                                     g->rev.col, g->reach, ll);
-    k_level_advance<<<1, 32, 0, c->stream>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode,
-                                             ll, c->lpool_cap, list_max_of(c));
+    k_fwd_push_step<K, false><<<push_grid<K>(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->seen,
+                                                                           c->msigma, c->ctrs, ll, nullptr);
+    k_fwd_pull_step<K, false><<<pull_grid<K>(c), BATCH_TPB, 0, c->stream>>>(g->rev, c->bi, c->fmtab, c->seen,
+                                                                           c->msigma, c->ctrs, ll, nullptr);
+    k_stats_step<K><<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->fwd.col, g->rev.col,
+                                                        g->reach, ll);
+    k_level_advance<K><<<1, 32, 0, c->stream>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode, ll,
+                                                c->lpool_cap, list_max_of(c));
 }
 
-static void bwd_step_kernels(axbc_ctx *c)
+template <int K> static void bwd_step_kernels(axbc_ctx *c)
 {
     axbc_graph *g = c->g;
-    k_bwd_step<false><<<bwd_grid(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma,
-                                                                c->mdelta, c->mq, c->mpartial, g->reach,
-                                                                c->ctrs, lists_of(c), nullptr);
+    k_bwd_step<K, false><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma,
+                                                                     c->mdelta, c->mq, c->mpartial, g->reach,
+                                                                     c->ctrs, lists_of(c), nullptr);
     if (g->fwd.n_heavy)
-        k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, c->stream>>>(
-            g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach,
-            lists_of(c));
+        k_bwd_combine_step<K><<<dim3((g->fwd.n_heavy + 7) / 8, K), 256, 0, c->stream>>>(
+            g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, lists_of(c));
     k_bwd_advance<<<1, 1, 0, c->stream>>>(c->bi);
 }
 
-// Capture one forward step and one backward step as CUDA graphs; every
-// argument is fixed for the context (levels come from device state).
-static int capture_steps(axbc_ctx *c, int dgrid, int sgrid)
+static void drop_captures(axbc_ctx *c)
 {
-    if (c->fwd_step_exec && c->bwd_step_exec) return AXBC_OK;
+    for (int i = 0; i < 2; i++) {
+        if (c->fwd_step_exec[i]) cudaGraphExecDestroy(c->fwd_step_exec[i]);
+        if (c->bwd_step_exec[i]) cudaGraphExecDestroy(c->bwd_step_exec[i]);
+        c->fwd_step_exec[i] = c->bwd_step_exec[i] = nullptr;
+    }
+}
+
+// Capture one forward step and one backward step of width K as CUDA graphs;
+// every argument is fixed for the context (levels come from device state).
+template <int K> static int capture_steps(axbc_ctx *c, int sgrid)
+{
+    const int i = K - 1;
+    if (c->fwd_step_exec[i] && c->bwd_step_exec[i]) return AXBC_OK;
     for (int which = 0; which < 2; which++) {
         cudaGraph_t gr = nullptr;
         CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        if (which == 0) fwd_step_kernels(c, dgrid, sgrid);
-        else bwd_step_kernels(c);
+        if (which == 0) fwd_step_kernels<K>(c, sgrid);
+        else bwd_step_kernels<K>(c);
         cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
         if (e != cudaSuccess) return axbc_cuda_fail(e, "capture level step", __FILE__, __LINE__);
-        e = cudaGraphInstantiate(which == 0 ? &c->fwd_step_exec : &c->bwd_step_exec, gr, 0);
+        e = cudaGraphInstantiate(which == 0 ? &c->fwd_step_exec[i] : &c->bwd_step_exec[i], gr, 0);
         cudaGraphDestroy(gr);
         if (e != cudaSuccess) return axbc_cuda_fail(e, "instantiate level step", __FILE__, __LINE__);
     }
@@ -1607,7 +1803,7 @@ static int capture_steps(axbc_ctx *c, int dgrid, int sgrid)
 // graph replays of one level step, in blocks (profiling and counting: each
 // kernel launched on its own).  *L_out: the first level that discovered
 // nothing.
-static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L_out)
+template <int K> static int traverse_stepwise(axbc_ctx *c, int nsrc, int sgrid, int *L_out)
 {
     axbc_graph *g = c->g;
     const uint64_t n = g->n;
@@ -1622,59 +1818,59 @@ static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L
     // forward steps launched before the first look at `alive`: one more than
     // the last batch needed, so a batch like it ends after one host round
     // trip; later groups double
-    int launched = 0, K = std::max(4, std::min(256, c->last_batch_levels + 1));
-    if (c->last_batch_levels == 0) K = 8;
+    int launched = 0, B = std::max(4, std::min(256, c->last_batch_levels + 1));
+    if (c->last_batch_levels == 0) B = 8;
     for (;;) {
-        TRY(axbc_batch_levels_alloc(c, launched + K + 2));
-        for (int i = 0; i < K; i++) {
+        TRY(axbc_batch_levels_alloc(c, launched + B + 2));
+        for (int i = 0; i < B; i++) {
             if (!prof) {
-                CU(cudaGraphLaunch(c->fwd_step_exec, s));
+                CU(cudaGraphLaunch(c->fwd_step_exec[K - 1], s));
             } else {
                 const int L = launched + i + 1;
                 {
                     ProfScope ps(c, KP_FWD_PUSH, 0);
                     if (c->prof_on) c->prof.back().tag = L;
                     if (wc)
-                        k_fwd_push_step<true><<<dgrid, BATCH_TPB, 0, s>>>(
+                        k_fwd_push_step<K, true><<<push_grid<K>(c), BATCH_TPB, 0, s>>>(
                             g->fwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PUSH * WC_NFIELDS);
                     else
-                        k_fwd_push_step<false><<<dgrid, BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->seen,
-                                                                           c->msigma, c->ctrs, ll, nullptr);
+                        k_fwd_push_step<K, false><<<push_grid<K>(c), BATCH_TPB, 0, s>>>(
+                            g->fwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
                 }
                 {
                     ProfScope ps(c, KP_FWD_PULL, 0);
                     if (c->prof_on) c->prof.back().tag = L;
                     if (wc)
-                        k_fwd_pull_step<true><<<pull_grid(c), BATCH_TPB, 0, s>>>(
+                        k_fwd_pull_step<K, true><<<pull_grid<K>(c), BATCH_TPB, 0, s>>>(
                             g->rev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PULL * WC_NFIELDS);
                     else
-                        k_fwd_pull_step<false><<<pull_grid(c), BATCH_TPB, 0, s>>>(
+                        k_fwd_pull_step<K, false><<<pull_grid<K>(c), BATCH_TPB, 0, s>>>(
                             g->rev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
                 }
                 {
                     ProfScope ps(c, KP_LEVEL_STATS, 0);
                     if (c->prof_on) c->prof.back().tag = L;
-                    k_stats_step<<<sgrid, BATCH_TPB, 0, s>>>(n, c->bi, c->fmtab, c->seen, g->fwd.col,
-                                                             g->rev.col, g->reach, ll);
+                    k_stats_step<K><<<sgrid, BATCH_TPB, 0, s>>>(n, c->bi, c->fmtab, c->seen, g->fwd.col,
+                                                                g->rev.col, g->reach, ll);
                 }
-                k_level_advance<<<1, 32, 0, s>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode,
-                                                 ll, c->lpool_cap, lmax);
+                k_level_advance<K><<<1, 32, 0, s>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode, ll,
+                                                    c->lpool_cap, lmax);
                 c->launches++;
             }
         }
         CU_LAUNCH("forward levels");
-        if (!prof) c->launches += 4ull * K;
-        launched += K;
+        if (!prof) c->launches += 4ull * B;
+        launched += B;
         c->prev_lend = std::min(launched, (int)c->fmask.size() - 1);  // masks written so far
         CU(cudaMemcpyAsync((char *)c->bi_host + ctl_off, (char *)c->bi + ctl_off, ctl_len,
                            cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
         if (!c->bi_host->alive) break;
-        if (launched + 2 * K + 2 > AXBC_MAX_LEVELS) {
+        if (launched + 2 * B + 2 > AXBC_MAX_LEVELS) {
             axbc_set_error("traversal deeper than %d levels", AXBC_MAX_LEVELS - 2);
             return AXBC_ERR_RANGE;
         }
-        K = std::min(2 * K, 256);
+        B = std::min(2 * B, 256);
     }
     const int L = c->bi_host->lend, Dmax = c->bi_host->dmax;
     *L_out = L;
@@ -1690,7 +1886,7 @@ static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L
         CU(cudaMemcpyAsync(lte.data(), c->d_level_te, (L + 1) * 8, cudaMemcpyDeviceToHost, s));
         CU(cudaMemcpyAsync(lcnt.data(), c->d_level_cnt, (L + 1) * 8, cudaMemcpyDeviceToHost, s));
         CU(cudaMemcpyAsync(lmode.data(), c->d_level_mode, (L + 1) * 4, cudaMemcpyDeviceToHost, s));
-        CU(cudaMemcpyAsync(&c->bi_host->depth0mask, &c->bi->depth0mask, 4, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(&c->bi_host->depth0mask, &c->bi->depth0mask, 8, cudaMemcpyDeviceToHost, s));
         CU(cudaStreamSynchronize(s));
         const double W = nsrc;
         for (size_t i = prof_first; i < c->prof.size(); i++) {
@@ -1707,11 +1903,11 @@ static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L
     }
 
     // backward: depths Dmax .. 0 (depth 0 only for pivots whose BFS ended at level 2)
-    uint32_t depth0 = 0;
+    unsigned long long depth0 = 0;
     if (Dmax >= 0) {
         for (int d = Dmax; d >= 0; d--) {
             if (!prof) {
-                CU(cudaGraphLaunch(c->bwd_step_exec, s));
+                CU(cudaGraphLaunch(c->bwd_step_exec[K - 1], s));
                 c->launches += g->fwd.n_heavy ? 3 : 2;
                 continue;
             }
@@ -1721,7 +1917,7 @@ static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L
             if (c->prof_on) {
                 double te_d = (double)lte[d], cnt_d = (double)lcnt[d];
                 if (d == 0) {
-                    const double frac = (double)__builtin_popcount(depth0) / W;
+                    const double frac = (double)__builtin_popcountll(depth0) / W;
                     te_d *= frac;
                     cnt_d *= frac;
                 }
@@ -1731,19 +1927,18 @@ static int traverse_stepwise(axbc_ctx *c, int nsrc, int dgrid, int sgrid, int *L
                 ProfScope ps(c, KP_BWD, bytes);
                 if (c->prof_on) c->prof.back().tag = d;
                 if (wc)
-                    k_bwd_step<true><<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma,
-                                                                      c->mdelta, c->mq, c->mpartial, g->reach,
-                                                                      c->ctrs, ll, wc + KP_BWD * WC_NFIELDS);
+                    k_bwd_step<K, true><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, s>>>(
+                        g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, c->ctrs, ll,
+                        wc + KP_BWD * WC_NFIELDS);
                 else
-                    k_bwd_step<false><<<bwd_grid(c), BATCH_TPB, 0, s>>>(g->fwd, c->bi, c->fmtab, c->msigma,
-                                                                       c->mdelta, c->mq, c->mpartial, g->reach,
-                                                                       c->ctrs, ll, nullptr);
+                    k_bwd_step<K, false><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, s>>>(
+                        g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, c->ctrs, ll,
+                        nullptr);
             }
             if (g->fwd.n_heavy) {
                 ProfScope ps(c, KP_BWD_COMBINE, 0);
-                k_bwd_combine_step<<<(g->fwd.n_heavy + 7) / 8, 256, 0, s>>>(
-                    g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach,
-            lists_of(c));
+                k_bwd_combine_step<K><<<dim3((g->fwd.n_heavy + 7) / 8, K), 256, 0, s>>>(
+                    g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, ll);
             }
             k_bwd_advance<<<1, 1, 0, s>>>(c->bi);
             c->launches++;
@@ -1773,13 +1968,13 @@ static bool use_persist(axbc_ctx *c, int nsrc)
 // block that fits resident (at most persist_blocks_per_sm per SM).  Level masks
 // are allocated up front for the last batch's depth and grown when the loop
 // asks for more.  *L_out: the first level that discovered nothing.
-static int traverse_persistent(axbc_ctx *c, int *L_out)
+template <int K> static int traverse_persistent(axbc_ctx *c, int *L_out)
 {
     axbc_graph *g = c->g;
     cudaStream_t s = c->stream;
     ALLOC_MISSING(c->gsync, sizeof(GridSync), &c->bytes);
     int bps = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_traverse_persist, BATCH_TPB, 0));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_traverse_persist<K>, BATCH_TPB, 0));
     bps = std::min(bps, std::max(1, c->persist_blocks_per_sm));
     if (bps < 1) {
         axbc_set_error("persistent level loop: no block of it fits on an SM");
@@ -1807,7 +2002,7 @@ static int traverse_persistent(axbc_ctx *c, int *L_out)
                         (void *)&c->gsync, (void *)&budget};
         {
             ProfScope ps(c, KP_PERSIST, 0);
-            CU(cudaLaunchCooperativeKernel((const void *)k_traverse_persist, grid, BATCH_TPB, args, 0, s));
+            CU(cudaLaunchCooperativeKernel((const void *)k_traverse_persist<K>, grid, BATCH_TPB, args, 0, s));
         }
         CU_LAUNCH("k_traverse_persist");
         CU(cudaMemcpyAsync(&hs, c->gsync, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
@@ -1831,36 +2026,42 @@ static int traverse_persistent(axbc_ctx *c, int *L_out)
     return AXBC_OK;
 }
 
-// Forward and backward passes of the batch whose roots/p are in c->bi.  The
-// host launches forward level steps in blocks (8, then doubling) and reads
-// the level state once per block; steps past the last level do nothing.
-int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
+// Forward and backward passes of the batch of width K whose roots/p are in
+// c->bi.  The host launches forward level steps in blocks (8, then doubling)
+// and reads the level state once per block; steps past the last level do
+// nothing.
+template <int K> static int batch_traverse(axbc_ctx *c, int nsrc, int H)
 {
     axbc_graph *g = c->g;
     const uint64_t n = g->n;
     cudaStream_t s = c->stream;
     const int sgrid = axbc_grid_for(c, BATCH_TPB, 8);
-    const int dgrid = dyn_grid(c);
+    TRY(occupancy<K>(c));
     // per-launch mode: profiling events around each kernel, or the counting builds
     const bool prof = c->prof_on || c->count_on;
     TRY(ensure_level_tables(c));
     TRY(axbc_batch_levels_alloc(c, 10));
-    if (!prof) TRY(capture_steps(c, dgrid, sgrid));
+    if (!prof) TRY(capture_steps<K>(c, sgrid));
 
-    // the previous batch's level masks back to zero, then a larger list pool
-    // if that batch ran out of list space
+    // the previous batch's level masks back to zero (in its own width), then a
+    // larger list pool if that batch ran out of list space
     if (c->prev_lend >= 2) {
-        k_clean_levels<<<axbc_grid_for(c, 256, 2), 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount,
-                                                              c->lcap, n, 2, c->prev_lend);
+        if (c->last_batch_k == 2)
+            k_clean_levels<2><<<axbc_grid_for(c, 256, 2), 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount,
+                                                                     c->lcap, n, 2, c->prev_lend);
+        else
+            k_clean_levels<1><<<axbc_grid_for(c, 256, 2), 256, 0, s>>>(c->fmtab, c->lpool, c->lstart, c->lcount,
+                                                                     c->lcap, n, 2, c->prev_lend);
         CU_LAUNCH("k_clean_levels");
         c->launches++;
     }
     c->prev_lend = 0;
     TRY(axbc_batch_settle(c));
-    if (c->pool_short && c->lpool_cap < 32 * n + 64) {
+    const uint64_t pool_limit = (uint64_t)AXBC_WMAX * n + 64;
+    if (c->pool_short && c->lpool_cap < pool_limit) {
         // the larger pool is allocated before the old one goes, so a failed
         // allocation leaves the context with a usable (smaller) pool
-        const uint32_t ncap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, 32 * n + 64),
+        const uint32_t ncap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(4ull * c->lpool_cap, pool_limit),
                                                            0xffffffffull);
         uint32_t *np = nullptr;
         TRY(axbc_dalloc((void **)&np, (uint64_t)ncap * 4, &c->bytes));
@@ -1869,34 +2070,32 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
         c->lpool = np;
         c->lpool_cap = ncap;
         c->pool_short = false;
-        if (c->fwd_step_exec) cudaGraphExecDestroy(c->fwd_step_exec);
-        if (c->bwd_step_exec) cudaGraphExecDestroy(c->bwd_step_exec);
-        c->fwd_step_exec = c->bwd_step_exec = nullptr;
-        if (!prof) TRY(capture_steps(c, dgrid, sgrid));
+        drop_captures(c);
+        if (!prof) TRY(capture_steps<K>(c, sgrid));
     }
-    CU(cudaMemsetAsync(c->seen, 0, n * 4, s));
-    CU(cudaMemsetAsync(c->fmask[0], 0, n * 4, s));
-    CU(cudaMemsetAsync(c->fmask[1], 0, n * 4, s));
-    CU(cudaMemsetAsync(c->msigma, 0, n * AXBC_W * 4, s));
-    CU(cudaMemsetAsync(c->ctrs, 0, 2 * AXBC_MAX_LEVELS * 4, s));
+    c->last_batch_k = K;
+    CU(cudaMemsetAsync(c->seen, 0, n * 4 * K, s));
+    CU(cudaMemsetAsync(c->fmask[0], 0, n * 4 * K, s));
+    CU(cudaMemsetAsync(c->fmask[1], 0, n * 4 * K, s));
+    CU(cudaMemsetAsync(c->msigma, 0, n * AXBC_W * K * 4, s));
+    CU(cudaMemsetAsync(c->ctrs, 0, 2 * AXBC_WMAX / 32 * AXBC_MAX_LEVELS * 4, s));
     CU(cudaMemsetAsync(c->lcount, 0, AXBC_MAX_LEVELS * 4, s));
     CU(cudaMemsetAsync(c->lheavy, 0, AXBC_MAX_LEVELS * 4, s));
     const LevelLists ll = lists_of(c);
     const uint32_t lmax = list_max_of(c);
     {
         ProfScope ps(c, KP_LEVEL_STATS, 0);
-        k_batch_init<<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
-                                      g->rev.col, g->m, c->push_factor_batch,
-                                      // a factor of 1e30 or more pulls every level
-                                      c->push_factor_batch >= 1e30 ? 0ull : (unsigned long long)(n / 4),
-                                      c->d_level_te,
-                                      c->d_level_cnt, ll, c->lpool_cap, lmax);
+        k_batch_init<K><<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
+                                         g->rev.col, g->m, c->push_factor_batch,
+                                         // a factor of 1e30 or more pulls every level
+                                         c->push_factor_batch >= 1e30 ? 0ull : (unsigned long long)(n / 4),
+                                         c->d_level_te, c->d_level_cnt, ll, c->lpool_cap, lmax);
     }
     CU_LAUNCH("k_batch_init");
 
     int L = 0;
-    if (use_persist(c, nsrc)) TRY(traverse_persistent(c, &L));
-    else TRY(traverse_stepwise(c, nsrc, dgrid, sgrid, &L));
+    if (use_persist(c, nsrc)) TRY(traverse_persistent<K>(c, &L));
+    else TRY(traverse_stepwise<K>(c, nsrc, sgrid, &L));
     // the per-pivot level counts and the list-pool flag arrive in the
     // background; the next batch (or a caller that reports them) waits for them
     if (!c->rb_ev) CU(cudaEventCreateWithFlags(&c->rb_ev, cudaEventDisableTiming));
@@ -1910,47 +2109,65 @@ int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
     return AXBC_OK;
 }
 
+// A multi-source pass of nsrc <= 64 pivots: 32-bit masks up to 32 pivots,
+// 64-bit masks above.
+int axbc_batch_traverse(axbc_ctx *c, int nsrc, int H)
+{
+    if (nsrc < 1 || nsrc > AXBC_WMAX) {
+        axbc_set_error("batched pass of %d pivots (1..%d)", nsrc, AXBC_WMAX);
+        return AXBC_ERR_INVALID;
+    }
+    return width_k(nsrc) == 2 ? batch_traverse<2>(c, nsrc, H) : batch_traverse<1>(c, nsrc, H);
+}
+
 int axbc_batch_settle(axbc_ctx *c)
 {
     if (!c->rb_pending) return AXBC_OK;
     CU(cudaEventSynchronize(c->rb_ev));
     c->rb_pending = false;
     c->pool_short = c->bi_host->pool_short != 0;
-    for (int i = 0; i < AXBC_W; i++) c->last_Ls[i] = i < c->last_batch_nsrc ? c->bi_host->Ls[i] : 0;
+    for (int i = 0; i < AXBC_WMAX; i++) c->last_Ls[i] = i < c->last_batch_nsrc ? c->bi_host->Ls[i] : 0;
     return AXBC_OK;
 }
 
 // The update of the applied lanes into each lane's bc vector, then the last
 // applied dependency vector of each lane segment [lane_lo[i], lane_hi[i]) into
 // delta_out[i] (defaults: one segment of all lanes into the context's).
-int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo,
-                           const int *lane_hi, int nseg)
+template <int K>
+static int apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo, const int *lane_hi, int nseg)
 {
     axbc_graph *g = c->g;
     cudaStream_t s = c->stream;
     // a grid-stride loop: exactly the blocks that stay resident
-    if (!c->upd_blocks_per_sm) {
+    if (!c->upd_blocks_per_sm[K - 1]) {
         int b = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_update_m, UPD_TPB, 0));
-        c->upd_blocks_per_sm = std::max(1, b);
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_update_m<K>, UPD_TPB(K), 0));
+        c->upd_blocks_per_sm[K - 1] = std::max(1, b);
     }
-    const int grid = axbc_grid_for(c, UPD_TPB, c->upd_blocks_per_sm);
-    const bool one_seg = nseg == 1 && (!lane_lo || lane_lo[0] == 0) && (!lane_hi || lane_hi[0] >= AXBC_W);
+    const int grid = axbc_grid_for(c, UPD_TPB(K), c->upd_blocks_per_sm[K - 1]);
+    const bool one_seg = nseg == 1 && (!lane_lo || lane_lo[0] == 0) && (!lane_hi || lane_hi[0] >= AXBC_W * K);
     {
         ProfScope ps(c, KP_UPDATE, (double)g->n * c->last_batch_nsrc * 20.0);
         // one segment over all lanes: the update writes the last delta itself
-        k_update_m<<<grid, UPD_TPB, 0, s>>>(c->mdelta, c->seen, g->reach, g->n, c->bi,
-                                            one_seg ? (delta_out ? delta_out[0] : c->delta_last) : nullptr);
+        k_update_m<K><<<grid, UPD_TPB(K), 0, s>>>(c->mdelta, c->seen, g->reach, g->n, c->bi,
+                                                  one_seg ? (delta_out ? delta_out[0] : c->delta_last) : nullptr);
     }
     for (int i = 0; i < nseg && !one_seg; i++) {
         ProfScope ps(c, KP_UPDATE, 0);
-        k_extract_delta<<<grid, 256, 0, s>>>(delta_out ? delta_out[i] : c->delta_last, c->mdelta,
-                                              c->seen, g->reach, g->n, c->bi,
-                                              lane_lo ? lane_lo[i] : 0, lane_hi ? lane_hi[i] : AXBC_W);
+        k_extract_delta<K><<<grid, 256, 0, s>>>(delta_out ? delta_out[i] : c->delta_last, c->mdelta, c->seen,
+                                                g->reach, g->n, c->bi, lane_lo ? lane_lo[i] : 0,
+                                                lane_hi ? lane_hi[i] : AXBC_WMAX);
     }
     CU_LAUNCH("update");
     c->delta_last_valid = true;
     return AXBC_OK;
+}
+
+int axbc_batch_apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo,
+                           const int *lane_hi, int nseg)
+{
+    return c->last_batch_k == 2 ? apply_lanes<2>(c, delta_out, lane_lo, lane_hi, nseg)
+                                : apply_lanes<1>(c, delta_out, lane_lo, lane_hi, nseg);
 }
 
 // Per forward level of the last batch: vertices newly reached (over all
@@ -1977,14 +2194,15 @@ int axbc_batch_apply(axbc_ctx *c) { return axbc_batch_apply_lanes(c, nullptr, nu
 
 __global__ void k_set_lane_targets(BatchInfo *bi, LaneTargets t)
 {
-    if (threadIdx.x < AXBC_W) bi->lane_bc[threadIdx.x] = t.bc[threadIdx.x];
+    if (threadIdx.x < AXBC_WMAX) bi->lane_bc[threadIdx.x] = t.bc[threadIdx.x];
 }
 
+// bc_of_lane: AXBC_WMAX vectors, one per lane of the pass
 int axbc_batch_set_targets(axbc_ctx *c, float *const *bc_of_lane)
 {
     LaneTargets t;
-    for (int i = 0; i < AXBC_W; i++) t.bc[i] = bc_of_lane[i];
-    k_set_lane_targets<<<1, AXBC_W, 0, c->stream>>>(c->bi, t);
+    for (int i = 0; i < AXBC_WMAX; i++) t.bc[i] = bc_of_lane[i];
+    k_set_lane_targets<<<1, AXBC_WMAX, 0, c->stream>>>(c->bi, t);
     CU_LAUNCH("k_set_lane_targets");
     return AXBC_OK;
 }
@@ -1993,7 +2211,7 @@ extern "C" int axbc_run_batch(axbc_ctx *c, const uint32_t *v0, const double *p, 
                               axbc_pivot_stats *stats)
 {
     CHECK_ARG(c && v0 && p, "axbc_run_batch: null argument");
-    CHECK_ARG(k >= 1 && k <= AXBC_MAX_BATCH, "axbc_run_batch: k must be in [1, 32]");
+    CHECK_ARG(k >= 1 && k <= AXBC_MAX_BATCH, "axbc_run_batch: k must be in [1, 64]");
     CHECK_ARG(H == 0 || H == 1, "axbc_run_batch: H must be 0 or 1");
     for (int i = 0; i < k; i++) CHECK_ARG(v0[i] < c->g->n, "axbc_run_batch: pivot >= n");
     TRY(axbc_ensure_batch(c));
@@ -2042,12 +2260,15 @@ extern "C" int axbc_get_batch_source(axbc_ctx *c, int src, uint32_t *sigma_host,
     TRY(axbc_dalloc((void **)&lvl, n * 4, nullptr));
     TRY(axbc_dalloc((void **)&dl, n * 4, nullptr));
     CU(cudaMemcpyAsync(d_fm, c->fmask.data(), levels * sizeof(uint32_t *), cudaMemcpyHostToDevice, s));
-    uint32_t depth0 = 0;
-    CU(cudaMemcpyAsync(&depth0, &c->bi->depth0mask, 4, cudaMemcpyDeviceToHost, s));
+    unsigned long long depth0 = 0;
+    CU(cudaMemcpyAsync(&depth0, &c->bi->depth0mask, 8, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
-    k_source_view<<<axbc_grid_for(c, 256, 4), 256, 0, s>>>(src, levels, d_fm, c->seen, c->msigma,
-                                                           c->mdelta, c->g->reach, n, depth0, sig,
-                                                           lvl, dl);
+    if (c->last_batch_k == 2)
+        k_source_view<2><<<axbc_grid_for(c, 256, 4), 256, 0, s>>>(src, levels, d_fm, c->seen, c->msigma, c->mdelta,
+                                                                  c->g->reach, n, depth0, sig, lvl, dl);
+    else
+        k_source_view<1><<<axbc_grid_for(c, 256, 4), 256, 0, s>>>(src, levels, d_fm, c->seen, c->msigma, c->mdelta,
+                                                                  c->g->reach, n, depth0, sig, lvl, dl);
     CU_LAUNCH("k_source_view");
     if (sigma_host) CU(cudaMemcpyAsync(sigma_host, sig, n * 4, cudaMemcpyDeviceToHost, s));
     if (lvl_host) CU(cudaMemcpyAsync(lvl_host, lvl, n * 4, cudaMemcpyDeviceToHost, s));

@@ -19,7 +19,8 @@
 #define AXBC_CHUNK 32
 #define AXBC_SPAN 1024
 #define AXBC_SAMPLE_BLOCK 1024
-#define AXBC_W 32
+#define AXBC_W 32     // lanes of a warp, pivots per mask word
+#define AXBC_WMAX 64  // pivots of one multi-source pass (two mask words per vertex)
 #define FULL_MASK 0xffffffffu
 
 // ---------------------------------------------------------------- errors
@@ -117,19 +118,20 @@ struct PivotCounters {  // device, single-source
     unsigned long long visited_rdeg;  // in-degree sum of visited vertices
 };
 
-struct BatchInfo {  // device, one multi-source batch
+struct BatchInfo {  // device, one multi-source batch of up to AXBC_WMAX pivots
     uint32_t nsrc;
-    uint32_t applymask;   // sources whose update is applied (Bader replay)
-    uint32_t srcmask;
-    uint32_t depth0mask;  // sources whose BFS ended at level 2
-    uint32_t root[AXBC_W];
-    double p[AXBC_W];
+    uint32_t pad0;
+    unsigned long long applymask;   // sources whose update is applied (Bader replay)
+    unsigned long long srcmask;
+    unsigned long long depth0mask;  // sources whose BFS ended at level 2
+    uint32_t root[AXBC_WMAX];
+    double p[AXBC_WMAX];
     // per-source totals accumulated by the level-stats kernel
-    unsigned long long nvis[AXBC_W];
-    unsigned long long rsum[AXBC_W];
-    unsigned long long te[AXBC_W];
+    unsigned long long nvis[AXBC_WMAX];
+    unsigned long long rsum[AXBC_WMAX];
+    unsigned long long te[AXBC_WMAX];
     // per-level scratch read back by the host
-    unsigned long long lvl_new[AXBC_W];
+    unsigned long long lvl_new[AXBC_WMAX];
     unsigned long long front_deg;
     unsigned long long unvis_deg;   // in-degree sum of vertices some pivot has not seen
     unsigned long long unvis_dec;   // this level's decrease of unvis_deg
@@ -147,15 +149,15 @@ struct BatchInfo {  // device, one multi-source batch
     int32_t push_next;  // 1: the next forward level pushes from the frontier
     double push_factor;
     unsigned long long push_min;  // frontier degree sums below this always push
-    int32_t Ls[AXBC_W];  // per pivot: first level that discovered nothing
+    int32_t Ls[AXBC_WMAX];  // per pivot: first level that discovered nothing
     int32_t pool_short;  // a level's list was capped by the pool's size
     int32_t pad_;
-    float *lane_bc[AXBC_W];  // per pivot: the bc vector its update goes to
+    float *lane_bc[AXBC_WMAX];  // per pivot: the bc vector its update goes to
 };
 
 // the bc vector of each lane, for a pass whose lanes belong to several runs
 struct LaneTargets {
-    float *bc[AXBC_W];
+    float *bc[AXBC_WMAX];
 };
 
 // capacity of the per-level tables of a context (levels of one traversal)
@@ -241,11 +243,13 @@ struct axbc_ctx {
     uint32_t lpool_cap = 0;
     bool pool_short = false;  // the last batch ran out of list space
     int prev_lend = 0;        // levels of the last batch whose masks need clearing
-    cudaGraphExec_t fwd_step_exec = nullptr;  // captured forward level step
-    cudaGraphExec_t bwd_step_exec = nullptr;  // captured backward level step
+    // captured forward / backward level steps, per width (index K - 1)
+    cudaGraphExec_t fwd_step_exec[2] = {nullptr, nullptr};
+    cudaGraphExec_t bwd_step_exec[2] = {nullptr, nullptr};
     int last_batch_levels = 0;
     int last_batch_nsrc = 0;
-    int last_Ls[AXBC_W] = {0};  // first empty level of each pivot of the last batch
+    int last_batch_k = 1;  // mask words per vertex of the last batch (1: <= 32 pivots, 2: <= 64)
+    int last_Ls[AXBC_WMAX] = {0};  // first empty level of each pivot of the last batch
     // the last batch's per-pivot level counts and list-pool flag are read back
     // without waiting; rb_ev marks their arrival (axbc_batch_settle)
     cudaEvent_t rb_ev = nullptr;
@@ -286,10 +290,11 @@ struct axbc_ctx {
     double push_factor_batch = 8.0;
     uint64_t bytes = 0;
     int num_sms = 0;
-    int dyn_blocks_per_sm = 0;  // resident blocks of the dynamic kernels
-    int upd_blocks_per_sm = 0;  // resident blocks of the batched bc update
-    int pull_blocks_per_sm = 0; // resident blocks of the forward pull kernel
-    int bwd_blocks_per_sm = 0;  // resident blocks of the backward kernel
+    // resident blocks per SM, per width (index K - 1)
+    int dyn_blocks_per_sm[2] = {0, 0};   // forward push
+    int upd_blocks_per_sm[2] = {0, 0};   // batched bc update
+    int pull_blocks_per_sm[2] = {0, 0};  // forward pull
+    int bwd_blocks_per_sm[2] = {0, 0};   // backward
 };
 
 // graph.cu: sort adjacency keys ((column << 32) | row, all-ones = none), drop

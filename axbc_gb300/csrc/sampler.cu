@@ -549,18 +549,18 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
 }
 
 // Pivots [off, off + count) of a drawn round become lanes lane0 + 0.. of one
-// pass (count = min(nb - off, AXBC_W - lane0)).
+// pass (count = min(nb - off, AXBC_WMAX - lane0)).
 __global__ void k_load_pass(const SamplerState *ss, BatchInfo *bi, int off, int lane0)
 {
     const int s = threadIdx.x;
-    const int count = min(ss->nb - off, AXBC_W - lane0);
+    const int count = min(ss->nb - off, AXBC_WMAX - lane0);
     if (s < count) {
         bi->root[lane0 + s] = ss->v0[off + s];
         bi->p[lane0 + s] = ss->p[off + s];
     }
 }
 
-// After a pass (the drawn pivots [off, off + AXBC_W)): replay Bader's test
+// After a pass (the drawn pivots [off, off + AXBC_WMAX)): replay Bader's test
 // between its pivots, fix how many are applied, and account rounds, skips and
 // traversed edges.  The pass that ends the round also settles the degree-0
 // draws after its last pivot.
@@ -568,10 +568,10 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
                                const float *__restrict__ mdelta, const uint32_t *__restrict__ seen,
                                const uint32_t *__restrict__ reach, const uint32_t *__restrict__ checks,
                                float *b, uint32_t *hist_v, double *hist_p, uint64_t hist_cap,
-                               int off, int lane0)
+                               int off, int lane0, int K)
 {
     if (ss->done && ss->nb == 0) return;
-    const int nb = max(0, min(ss->nb - off, AXBC_W - lane0));
+    const int nb = max(0, min(ss->nb - off, AXBC_WMAX - lane0));
     const bool last = off + nb >= ss->nb;
     const uint64_t N = ss->N;
     const uint32_t c = ss->bader_c;
@@ -608,15 +608,16 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
                 if (rr > 0) b[i] = __fadd_rn(b[i], bc_root_term(rr, nvt));
                 continue;
             }
-            const float dv = ((seen[v] >> l) & 1u) ? mdelta[(uint64_t)v * AXBC_W + l]
-                                                   : __uint2float_rn(reach[v]);
+            // the pass's layout: K mask words and 32 K row values per vertex
+            const bool reached = (seen[(uint64_t)v * K + l / 32] >> (l % 32)) & 1u;
+            const float dv = reached ? mdelta[(uint64_t)v * (AXBC_W * K) + l] : __uint2float_rn(reach[v]);
             if (dv == 0.0f && p > 0.0) continue;
             b[i] = __fadd_rn(b[i], bc_term(dv, rr, p));
         }
     }
     // lanes [lane0, lane0 + nb) of the pass: the first `stop` are applied
-    const uint32_t seg = (nb >= 32 ? FULL_MASK : ((1u << nb) - 1u)) << lane0;
-    const uint32_t app = (stop >= 32 ? FULL_MASK : ((1u << stop) - 1u)) << lane0;
+    const unsigned long long seg = (nb >= 64 ? ~0ull : ((1ull << nb) - 1ull)) << lane0;
+    const unsigned long long app = (stop >= 64 ? ~0ull : ((1ull << stop) - 1ull)) << lane0;
     bi->applymask = (bi->applymask & ~seg) | app;
     ss->napply = stop;
     for (int s = 0; s < stop; s++) {
@@ -840,7 +841,7 @@ bool sr_finished(const SampledRun *r)
 
 int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0)
 {
-    k_load_pass<<<1, AXBC_W, 0, c->stream>>>(r->ss, c->bi, off, lane0);
+    k_load_pass<<<1, AXBC_WMAX, 0, c->stream>>>(r->ss, c->bi, off, lane0);
     CU_LAUNCH("k_load_pass");
     return AXBC_OK;
 }
@@ -851,7 +852,7 @@ int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0)
         ProfScope ps(c, KP_SAMPLER, 0);
         k_sampler_post<<<1, 1, 0, c->stream>>>(r->ss, c->bi, r->bc, c->mdelta, c->seen, c->g->reach,
                                                r->checks, r->checkval, r->hist_v, r->hist_p,
-                                               r->hist_cap, off, lane0);
+                                               r->hist_cap, off, lane0, c->last_batch_k);
     }
     CU_LAUNCH("k_sampler_post");
     return AXBC_OK;
@@ -920,28 +921,28 @@ static int ensure_sampler(axbc_ctx *c, uint32_t nchecks)
     return AXBC_OK;
 }
 
-// One drawn round of one run: its pivots in passes of at most AXBC_W lanes;
-// the Bader replay of each pass sees the bc of the passes before it.
+// One drawn round of one run: its pivots in one pass (widths up to 64); the
+// Bader replay between the pass's pivots decides how many are applied.
 static int sr_round_alone(axbc_ctx *c, SampledRun *r)
 {
     const int nb = sr_nb(r);
-    for (int off = 0; off == 0 || off < nb; off += AXBC_W) {
-        const int cnt = std::min(nb - off, AXBC_W);
+    for (int off = 0; off == 0 || off < nb; off += AXBC_WMAX) {
+        const int cnt = std::min(nb - off, AXBC_WMAX);
         if (cnt > 0) {
             TRY(sr_load(c, r, off, 0));
             TRY(axbc_batch_traverse(c, cnt, r->prm.H));
             r->batches++;
-            float *tg[AXBC_W];
-            for (int i = 0; i < AXBC_W; i++) tg[i] = r->bc;
+            float *tg[AXBC_WMAX];
+            for (int i = 0; i < AXBC_WMAX; i++) tg[i] = r->bc;
             TRY(axbc_batch_set_targets(c, tg));
         }
         TRY(sr_post(c, r, off, 0));
         if (cnt > 0) {
             float *dout[1] = {r->delta_last};
-            const int lo[1] = {0}, hi[1] = {AXBC_W};
+            const int lo[1] = {0}, hi[1] = {AXBC_WMAX};
             TRY(axbc_batch_apply_lanes(c, dout, lo, hi, 1));
         }
-        if (off + AXBC_W < nb) {
+        if (off + AXBC_WMAX < nb) {
             // a later pass runs only if Bader's test did not stop the round
             CU(cudaMemcpyAsync(&r->ss_host->done, &r->ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                c->stream));

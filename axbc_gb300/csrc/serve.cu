@@ -167,8 +167,8 @@ static int serve_pass(axbc_server *S, ServeGraph &G, std::vector<Request *> &run
     if (segs.empty()) return AXBC_OK;
     for (auto &sg : segs) TRY(sr_load(c, &sg.first->run, 0, sg.second));
     TRY(axbc_batch_traverse(c, lane, G.H));
-    float *tg[AXBC_W];
-    for (int i = 0; i < AXBC_W; i++) tg[i] = segs[0].first->run.bc;
+    float *tg[AXBC_WMAX];
+    for (int i = 0; i < AXBC_WMAX; i++) tg[i] = segs[0].first->run.bc;
     std::vector<float *> dout;
     std::vector<int> lo, hi;
     for (auto &sg : segs) {

@@ -35,10 +35,11 @@ enum {
     AXBC_ERR_BUSY = 7        /* serving: admission refused for lack of memory */
 };
 
-/* Batch width of the multi-source pass (sources per warp bitmask). */
-#define AXBC_MAX_BATCH 32
+/* Pivots of one multi-source pass: a 32-bit mask per vertex per level up to
+ * 32 pivots, a 64-bit mask up to 64 (a warp lane owns two pivots). */
+#define AXBC_MAX_BATCH 64
 /* largest sampling width of a sampled run: a round draws up to 64 pivots from
- * one snapshot and traverses them as passes of at most AXBC_MAX_BATCH */
+ * one snapshot and traverses them as one pass */
 #define AXBC_MAX_WIDTH 64
 
 typedef struct axbc_graph axbc_graph;
@@ -198,9 +199,9 @@ int axbc_bc_pivot_static(const uint32_t *col, const uint32_t *row, const uint32_
 
 /* ---- batched (multi-source) form ----
  * k <= AXBC_MAX_BATCH pivots in one multi-source pass (one bit per pivot in a
- * 32-bit mask per vertex; a pivot may repeat).  bc receives the pivots'
- * updates in list order, bit-identical to k calls of axbc_run_pivot.  stats
- * may be NULL. */
+ * 32-bit mask per vertex for k <= 32, a 64-bit mask above; a pivot may
+ * repeat).  bc receives the pivots' updates in list order, bit-identical to k
+ * calls of axbc_run_pivot.  stats may be NULL. */
 int axbc_run_batch(axbc_ctx *ctx, const uint32_t *v0, const double *p, int k, int H,
                    axbc_pivot_stats *stats);
 
@@ -252,7 +253,7 @@ int axbc_bader_check(axbc_ctx *ctx, const uint32_t *checks, uint32_t x, uint32_t
 /* ---- request server (many sampled runs over resident graphs) ----
  * The reference serves one job per process.  The server keeps graphs resident
  * and runs submitted sampled runs (the parameters of axbc_run_sampled, widths
- * 1..AXBC_MAX_BATCH) with one worker thread and stream per graph, packing the
+ * 1..32) with one worker thread and stream per graph, packing the
  * drawn rounds of the requests of one graph into the lanes of a shared
  * multi-source pass; passes on different graphs overlap on the device.  Each
  * request's bc, pivots and counters are bit-identical to axbc_run_sampled with

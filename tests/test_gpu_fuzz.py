@@ -71,7 +71,7 @@ def test_random_plain_and_batch_passes(axbc, orc, case):
     ctx = axbc.Context(G)
     f_plain, f_batch = (float(x) for x in rng.choice([0.0, 0.125, 1.0, 8.0, 1e30], size=2))
     ctx.set_tuning(f_plain, f_batch)
-    k = int(rng.integers(1, 33))
+    k = int(rng.integers(1, 65))
     piv = rng.integers(0, n, size=k).astype(np.uint32)
     p = rng.random(k) + 1e-3
     want, dl, te = orc.bc_pivots(g, piv, p, H)

@@ -75,7 +75,7 @@ def test_plain_push_only_and_pull_only(axbc, orc, factor):
 
 
 @pytest.mark.parametrize("H", [0, 1])
-@pytest.mark.parametrize("k", [1, 7, 32])
+@pytest.mark.parametrize("k", [1, 7, 32, 33, 64])
 def test_batch_bit_exact(axbc, orc, H, k):
     g, G = make(axbc, orc, golden_edges(), 1024, True, H)
     ctx = axbc.Context(G)
@@ -106,6 +106,16 @@ def test_batch_accumulates_across_calls(axbc, orc):
     ctx.run_batch(piv[32:], p[32:])
     want, _, _ = orc.bc_pivots(g, piv, p)
     assert_float_exact(ctx.bc(), want, "bc after two batches")
+    # widths alternating on one context (64-bit, 32-bit, 64-bit masks): the
+    # level masks left by each pass are cleared in the layout it used
+    more = pivots_of(g, 110, seed=10)
+    pm = np.full(110, 1.0 / 1024)
+    ctx.reset()
+    ctx.run_batch(more[:50], pm[:50])
+    ctx.run_batch(more[50:60], pm[50:60])
+    ctx.run_batch(more[60:110], pm[60:110])
+    want, _, _ = orc.bc_pivots(g, more, pm)
+    assert_float_exact(ctx.bc(), want, "bc after passes of 50, 10 and 50 pivots")
 
 
 def heavy_graph(seed=1):
@@ -125,9 +135,10 @@ def test_heavy_vertices_and_directed(axbc, orc, undirected):
     g, G = make(axbc, orc, e, n, undirected, 0)
     assert G.symmetric == undirected
     ctx = axbc.Context(G)
-    piv = pivots_of(g, 32, seed=2)
+    piv = pivots_of(g, 64, seed=2)
     piv[0] = 0
-    p = np.full(32, 1.0 / n)
+    piv[40] = 1
+    p = np.full(64, 1.0 / n)
     for factor in (0.0, 1.0, 1e30):
         ctx.set_tuning(factor, factor)
         ctx.reset()

@@ -65,13 +65,14 @@ def gs(axbc, orc):
     return graphs(axbc, orc)
 
 
+@pytest.mark.parametrize("k", [5, 32, 64])
 @pytest.mark.parametrize("name", ["grid128", "kron12", "kron11_H1", "kron10_directed", "strip"])
-def test_persistent_pass_equals_step_launches_and_oracle(axbc, orc, gs, name):
+def test_persistent_pass_equals_step_launches_and_oracle(axbc, orc, gs, name, k):
     G = gs[name]
     H = 1 if name.endswith("H1") else 0
     deg = G.deg()
     cand = np.flatnonzero(deg > 0)
-    piv = np.random.default_rng(7).choice(cand, size=min(32, len(cand)), replace=False).astype(np.uint32)
+    piv = np.random.default_rng(7 + k).choice(cand, size=min(k, len(cand)), replace=False).astype(np.uint32)
     p = np.full(len(piv), 1.0 / G.n)
     res = {}
     for mode in (-1, 1):
