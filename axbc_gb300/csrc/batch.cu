@@ -1385,26 +1385,24 @@ template <int N> __device__ __forceinline__ void cp_async_wait()
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// stage the dependency rows of the chunk's reached vertices: lane l copies
-// columns l + 32 h of each row
-template <int K, class M>
-__device__ __forceinline__ void stage_rows(float (*rows)[AXBC_W * K + 1], const float *__restrict__ mdelta,
-                                           uint64_t base, M sv)
+// stage the dependency rows of the chunk's vertices reached by pivots of half
+// hh (sv: their masks for that half): lane l copies column 32 hh + l
+template <int K>
+__device__ __forceinline__ void stage_half(float (*rows)[AXBC_W + 1], const float *__restrict__ mdelta,
+                                           uint64_t base, uint32_t sv, int hh)
 {
     const unsigned lane = lane_id();
     unsigned need = __ballot_sync(FULL_MASK, sv != 0);
     while (need) {
         const int r = __ffs(need) - 1;
         need &= need - 1;
-#pragma unroll
-        for (int h = 0; h < K; h++)
-            cp_async4(&rows[r][32 * h + lane], mdelta + row_base<K>(base + r) + 32 * h + lane);
+        cp_async4(&rows[r][lane], mdelta + row_base<K>(base + r) + 32 * hh + lane);
     }
     cp_async_commit();
 }
 
-// threads of the update: 128 (34 KB of staged rows) for 32 pivots, 64 for 64
-#define UPD_TPB(K) (128 / (K))
+// threads of the update (34 KB of staged rows)
+#define UPD_TPB(K) 128
 template <int K>
 __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict__ mdelta,
                                                          const uint32_t *__restrict__ seen_,
@@ -1426,10 +1424,10 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
     __shared__ float4 s_k[NS];
     __shared__ int s_single;  // every applied lane updates the same vector
     __shared__ int s_allpos;  // every applied lane has p > 0 (zero terms vanish)
-    // per warp, two chunks: the dependency rows of 32 vertices, padded to
-    // NS + 1 floats so that thread t reading row t, column s hits bank
-    // (t + s) mod 32
-    __shared__ float s_rows[TPB / 32][2][32][NS + 1];
+    // per warp, two staged units: the dependency rows of 32 vertices for one
+    // 32-pivot half, padded to 33 floats so that thread t reading row t,
+    // column s hits bank (t + s) mod 32
+    __shared__ float s_rows[TPB / 32][2][32][AXBC_W + 1];
     const M amask = (M)(bi->applymask & bi->srcmask);
     for (int s = threadIdx.x; s < NS; s += TPB) {
         s_bc[s] = bi->lane_bc[s];
@@ -1489,9 +1487,11 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
         sv = seen[base + lane];
         rv = reach[base + lane];
     }
-    stage_rows<K>(s_rows[wid][0], mdelta, base, sv);
-    for (int buf = 0; base < n; base += stride, buf ^= 1) {
-        // the next chunk's rows load while this chunk is summed
+    // units of (chunk of 32 vertices, 32-pivot half), in order; each vertex
+    // sums its slots in slot order across the halves of its chunk
+    stage_half<K>(s_rows[wid][0], mdelta, base, (uint32_t)sv, 0);
+    int buf = 0;
+    for (; base < n; base += stride) {
         const uint64_t next = base + stride;
         M svn = 0;
         uint32_t rvn = 0;
@@ -1499,86 +1499,93 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
             svn = seen[next + lane];
             rvn = reach[next + lane];
         }
-        if (next < n) {
-            stage_rows<K>(s_rows[wid][buf ^ 1], mdelta, next, svn);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncwarp();
         const uint64_t v = base + lane;
-        if (delta_out && v < n) {
-            const bool have = v == dl_root ? dl_root_done : ((sv >> slast) & 1u) != 0u;
-            delta_out[v] = have ? s_rows[wid][buf][lane][slast] : __uint2float_rn(rv);
-        }
+        const float rf = __uint2float_rn(rv);
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
         const bool work = v < n && (sv != 0 || rv != 0u || !skip_unreached);
-        if (work && single && rv == 0u && skip_unreached) {
-            // one target vector, reach 0, every p > 0: a pivot that did not
-            // reach v adds +0, so only the reached lanes are visited, in lane
-            // order (roots are reached by their own lane)
-            const float(*rows)[NS + 1] = s_rows[wid][buf];
-            float *tgt = s_bc[slast];
-            float b = tgt[v];
-            for (M bits = sv & amask; bits; bits &= bits - 1) {
-                const int s = __ffsll((unsigned long long)bits) - 1;
-                if ((uint32_t)v == s_root[s]) {
-                    if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
-                    continue;
-                }
-                const float dv = rows[lane][s];
-                if (dv == 0.0f) continue;
-                const float4 k = s_k[s];
-                const uint32_t fl = __float_as_uint(k.w);
-                b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
-            }
-            tgt[v] = b;
-        } else if (work && single) {
-            // one target vector: every slot in order
-            const float(*rows)[NS + 1] = s_rows[wid][buf];
-            const float rf = __uint2float_rn(rv);
-            float *tgt = s_bc[slast];
-            float b = tgt[v];
-#pragma unroll
-            for (int s = 0; s < NS; s++) {
-                if (!((amask >> s) & 1u)) continue;
-                if ((uint32_t)v == s_root[s]) {
-                    if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
-                    continue;
-                }
-                const float dv = ((sv >> s) & 1u) ? rows[lane][s] : rf;
-                const float4 k = s_k[s];
-                const uint32_t fl = __float_as_uint(k.w);
-                if (dv == 0.0f && (fl & 2u)) continue;
-                b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
-            }
-            tgt[v] = b;
-        } else if (work) {
-            const float(*rows)[NS + 1] = s_rows[wid][buf];
-            const float rf = __uint2float_rn(rv);
-            // lanes in order; consecutive lanes of one run add into one
-            // register, written back when the target vector changes
-            float *tgt = nullptr;
-            float b = 0.0f;
-            for (int s = 0; s <= slast; s++) {
-                if (!((amask >> s) & 1u)) continue;
-                if (s_bc[s] != tgt) {
-                    if (tgt) tgt[v] = b;
-                    tgt = s_bc[s];
-                    b = tgt[v];
-                }
-                if ((uint32_t)v == s_root[s]) {
-                    if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
-                    continue;
-                }
-                const float dv = ((sv >> s) & 1u) ? rows[lane][s] : rf;
-                if (dv == 0.0f && s_skip0[s]) continue;
-                b = __fadd_rn(b, bc_term_fast(dv, s_reach[s], s_p[s], s_iv[s]));
-            }
-            tgt[v] = b;
+        // one target vector, reach 0, every p > 0: a pivot that did not reach
+        // v adds +0, so only the reached lanes are visited
+        const bool sparse = work && single && rv == 0u && skip_unreached;
+        float *tgt = nullptr;
+        float b = 0.0f;
+        if (work && single) {
+            tgt = s_bc[slast];
+            b = tgt[v];
         }
-        __syncwarp();
+#pragma unroll 1
+        for (int hh = 0; hh < K; hh++, buf ^= 1) {
+            // the next unit's rows load while this one is summed
+            if (hh + 1 < K) {
+                stage_half<K>(s_rows[wid][buf ^ 1], mdelta, base, (uint32_t)((unsigned long long)sv >> 32), 1);
+                cp_async_wait<1>();
+            } else if (next < n) {
+                stage_half<K>(s_rows[wid][buf ^ 1], mdelta, next, (uint32_t)svn, 0);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+            const float(*rows)[AXBC_W + 1] = s_rows[wid][buf];
+            const uint32_t svh = (uint32_t)((unsigned long long)sv >> (32 * hh));
+            const uint32_t amh = (uint32_t)((unsigned long long)amask >> (32 * hh));
+            const int s0 = 32 * hh;
+            if (delta_out && v < n && (slast >> 5) == hh) {
+                const bool have = v == dl_root ? dl_root_done : ((svh >> (slast & 31)) & 1u) != 0u;
+                delta_out[v] = have ? rows[lane][slast & 31] : rf;
+            }
+            if (sparse) {
+                for (uint32_t bits = svh & amh; bits; bits &= bits - 1) {
+                    const int j = __ffs(bits) - 1, s = s0 + j;
+                    if ((uint32_t)v == s_root[s]) {
+                        if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
+                        continue;
+                    }
+                    const float dv = rows[lane][j];
+                    if (dv == 0.0f) continue;
+                    const float4 k = s_k[s];
+                    const uint32_t fl = __float_as_uint(k.w);
+                    b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
+                }
+            } else if (work && single) {
+                // one target vector: every slot in order
+#pragma unroll
+                for (int j = 0; j < AXBC_W; j++) {
+                    if (!((amh >> j) & 1u)) continue;
+                    const int s = s0 + j;
+                    if ((uint32_t)v == s_root[s]) {
+                        if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
+                        continue;
+                    }
+                    const float dv = ((svh >> j) & 1u) ? rows[lane][j] : rf;
+                    const float4 k = s_k[s];
+                    const uint32_t fl = __float_as_uint(k.w);
+                    if (dv == 0.0f && (fl & 2u)) continue;
+                    b = __fadd_rn(b, div_to_float_hl(__fmul_rn(dv, k.x), s_p[s], k.y, k.z, (fl & 1u) != 0u));
+                }
+            } else if (work) {
+                // lanes in order; consecutive lanes of one run add into one
+                // register, written back when the target vector changes
+                for (int j = 0; j < AXBC_W && s0 + j <= slast; j++) {
+                    if (!((amh >> j) & 1u)) continue;
+                    const int s = s0 + j;
+                    if (s_bc[s] != tgt) {
+                        if (tgt) tgt[v] = b;
+                        tgt = s_bc[s];
+                        b = tgt[v];
+                    }
+                    if ((uint32_t)v == s_root[s]) {
+                        if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
+                        continue;
+                    }
+                    const float dv = ((svh >> j) & 1u) ? rows[lane][j] : rf;
+                    if (dv == 0.0f && s_skip0[s]) continue;
+                    b = __fadd_rn(b, bc_term_fast(dv, s_reach[s], s_p[s], s_iv[s]));
+                }
+            }
+            __syncwarp();
+        }
+        if (tgt) tgt[v] = b;
         sv = svn;
         rv = rvn;
     }

@@ -160,7 +160,7 @@ static int serve_pass(axbc_server *S, ServeGraph &G, std::vector<Request *> &run
     int lane = 0;
     for (Request *r : ready) {
         const int nb = sr_nb(&r->run);
-        if (lane + nb > AXBC_W) continue;  // its drawn round waits for the next pass
+        if (lane + nb > AXBC_WMAX) continue;  // its drawn round waits for the next pass
         segs.push_back({r, lane});
         lane += nb;
     }
@@ -346,7 +346,7 @@ extern "C" int axbc_request_submit(axbc_server *S, int graph_id, const axbc_run_
         Gp = S->graphs[graph_id].get();
     }
     const ServeGraph &G = *Gp;
-    TRY(sr_check_params(G.g, prm, AXBC_W));
+    TRY(sr_check_params(G.g, prm, AXBC_WMAX));
     CHECK_ARG(prm->H == G.H, "axbc_request_submit: H differs from the graph's");
     auto r = std::make_unique<Request>();
     r->graph = graph_id;

@@ -47,7 +47,7 @@ def parse():
                          "(SIDE x SIDE grid, 2%% of edges dropped, 0.01%% long-range, seed 7)")
     ap.add_argument("--edgefactor", type=int, default=16)
     ap.add_argument("--pivots", type=int, default=1024, help="pivots per step")
-    ap.add_argument("--width", type=int, default=32, help="batch width")
+    ap.add_argument("--width", type=int, default=64, help="batch width")
     ap.add_argument("--z", type=int, default=3, help="sampling heuristic")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the oracle baseline sample")
@@ -206,7 +206,7 @@ def oracle_single(g_csc, pivots, probs):
 # The other benchmark configurations: graph, heuristic, budget, stop rule, width
 # (None: from the autotuner), one-degree reduction.
 CONFIGS = {
-    "config1": dict(graph=("kron", 14), H=0, z=0, nbfs=256, c=0, x=1, seed=1, W=32,
+    "config1": dict(graph=("kron", 14), H=0, z=0, nbfs=256, c=0, x=1, seed=1, W=64,
                     desc="Kronecker scale 14 (Graph500 generator, seeds 23/24), -H 0 -z 0 -N 256 -c 0"),
     "config2": dict(graph=("kron", 20), H=1, z=1, nbfs=4096, c=0, x=1, seed=1, W=64,
                     desc="Kronecker scale 20, -H 1 -z 1 -N 4096 -c 0, width 64"),

@@ -253,9 +253,9 @@ int axbc_bader_check(axbc_ctx *ctx, const uint32_t *checks, uint32_t x, uint32_t
 /* ---- request server (many sampled runs over resident graphs) ----
  * The reference serves one job per process.  The server keeps graphs resident
  * and runs submitted sampled runs (the parameters of axbc_run_sampled, widths
- * 1..32) with one worker thread and stream per graph, packing the
- * drawn rounds of the requests of one graph into the lanes of a shared
- * multi-source pass; passes on different graphs overlap on the device.  Each
+ * 1..AXBC_MAX_WIDTH) with one worker thread and stream per graph, packing the
+ * drawn rounds of the requests of one graph into the up to 64 lanes of a
+ * shared multi-source pass; passes on different graphs overlap on the device.  Each
  * request's bc, pivots and counters are bit-identical to axbc_run_sampled with
  * the same parameters.  Admission: a request's device state must fit in the
  * budget's remaining bytes; otherwise it waits in arrival order. */

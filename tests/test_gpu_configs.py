@@ -93,7 +93,7 @@ def test_config3_grid_sampled_adaptive_matches_oracle(axbc, orc, grid2048):
     same_floats(ctx.bc(), want["bc"], "grid sampled bc")
 
 
-@pytest.mark.parametrize("W", [1, 32])
+@pytest.mark.parametrize("W", [1, 32, 64])
 def test_config1_scale14_z0_sampled(axbc, orc, W):
     """Config 1: the reference's scale-14 graph (Graph500 generator, seeds
     23/24, built on the device), -H 0 -z 0 -N 256 -c 0, seed 1: the whole run

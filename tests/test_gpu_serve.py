@@ -21,7 +21,8 @@ def same_bits(got, want, what):
 
 # (z, W, seed, nbfs, bader_c, nchecks): widths add up to more than one pass
 MIX = [(0, 8, 1, 60, 0, 1), (3, 16, 2, 50, 0, 2), (4, 4, 3, 40, 0, 1), (1, 8, 4, 48, 0, 1),
-       (5, 8, 5, 40, 0, 1), (6, 8, 6, 40, 0, 2), (2, 1, 7, 12, 0, 1), (0, 32, 8, 200, 1, 8)]
+       (5, 8, 5, 40, 0, 1), (6, 8, 6, 40, 0, 2), (2, 1, 7, 12, 0, 1), (0, 32, 8, 200, 1, 8),
+       (4, 64, 9, 256, 1, 4), (3, 48, 10, 150, 0, 1)]
 
 
 @pytest.fixture(scope="module")
@@ -149,7 +150,7 @@ def test_random_request_mixes(axbc, orc, seed):
         gi = int(rng.integers(3))
         g, G, H, gid = graphs[gi]
         z = int(rng.integers(0, 7))
-        W = int(rng.choice([1, 4, 8, 16, 32]))
+        W = int(rng.choice([1, 4, 8, 16, 32, 64]))
         nbfs = int(rng.integers(1, min(g.n, 150)))
         c, x = (0, 1) if rng.random() < 0.6 else (1, int(rng.integers(1, 5)))
         sd = int(rng.integers(1, 1 << 30))
