@@ -47,7 +47,7 @@ def parse():
                          "(SIDE x SIDE grid, 2%% of edges dropped, 0.01%% long-range, seed 7)")
     ap.add_argument("--edgefactor", type=int, default=16)
     ap.add_argument("--pivots", type=int, default=1024, help="pivots per step")
-    ap.add_argument("--width", type=int, default=64, help="batch width")
+    ap.add_argument("--width", type=int, default=32, help="batch width (the headline configuration: batches of 32)")
     ap.add_argument("--z", type=int, default=3, help="sampling heuristic")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the oracle baseline sample")
@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--skip-plain", action="store_true", help="profiling runs: no plain pass")
     ap.add_argument("--skip-serving", action="store_true", help="no serving phase after the headline")
     ap.add_argument("--skip-count", action="store_true", help="no counted step (roofline bytes)")
+    ap.add_argument("--skip-wide", action="store_true", help="no width-64 leg after the headline")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "serving", "config1", "config2", "config3"],
                     help="serving: the request server on resident graphs (p50/p99 latency); "
@@ -135,23 +136,36 @@ def kernel_source_digest():
         return hashlib.sha256(f.read()).hexdigest()
 
 
-def traffic_for(kernel, graph_key):
-    """(per-launch DRAM bytes of `kernel` on this graph from the committed ncu
-    capture in profiles/traffic.json, note).  None when there is no capture for
-    this graph and kernel, or when it was taken of other kernel source."""
+def traffic_for(kernel, graph_key, must_per_launch, words):
+    """(per-launch DRAM bytes of `kernel`, note) from the committed ncu capture in
+    profiles/traffic.json.  The capture is of a smaller graph of the same family
+    (a few GB on the device); it records, per traversal kernel, DRAM bytes per
+    byte the kernel must move (its counting build over the same steps), and the
+    figure here is that ratio times this launch's must-move bytes.  None when
+    there is no capture for this graph family and kernel, when it was taken of
+    other kernel source, or without a must-move count.  `words`: mask words per
+    vertex of the passes (1 up to 32 pivots, 2 up to 64), the kernel build the
+    capture must be of."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
     except Exception:
         return None, "no ncu capture committed"
-    ent = t.get(graph_key, {})
-    k = ent.get("kernels", {}).get(kernel)
-    if k is None:
-        return None, f"no ncu capture of {kernel} on {graph_key}"
+    family = graph_key.split("-")[0]
+    ent = t.get(family, {})
+    k = ent.get("kernels", {}).get(f"{kernel}<{words}>")
+    if k is None or "dram_per_must_move_byte" not in k:
+        return None, f"no ncu capture of {kernel}<{words}> on a {family} graph"
     if ent.get("kernel_source_sha256") != kernel_source_digest():
         return None, "the committed ncu capture is of other kernel source (stale)"
-    return float(k["dram_bytes_per_launch"]), f"ncu capture at {ent.get('commit', '?')}"
+    if not must_per_launch:
+        return None, "no must-move count in this run"
+    r = float(k["dram_per_must_move_byte"])
+    return r * must_per_launch, (f"ncu capture of {kernel}<{words}> on {ent.get('graph')} at "
+                                 f"{ent.get('commit', '?')}: "
+                                 f"{r:.3f} DRAM bytes per must-move byte, times this launch's "
+                                 f"must-move bytes")
 
 
 class _DeviceArray:
@@ -206,7 +220,7 @@ def oracle_single(g_csc, pivots, probs):
 # The other benchmark configurations: graph, heuristic, budget, stop rule, width
 # (None: from the autotuner), one-degree reduction.
 CONFIGS = {
-    "config1": dict(graph=("kron", 14), H=0, z=0, nbfs=256, c=0, x=1, seed=1, W=64,
+    "config1": dict(graph=("kron", 14), H=0, z=0, nbfs=256, c=0, x=1, seed=1, W=32,
                     desc="Kronecker scale 14 (Graph500 generator, seeds 23/24), -H 0 -z 0 -N 256 -c 0"),
     "config2": dict(graph=("kron", 20), H=1, z=1, nbfs=4096, c=0, x=1, seed=1, W=64,
                     desc="Kronecker scale 20, -H 1 -z 1 -N 4096 -c 0, width 64"),
@@ -521,7 +535,7 @@ def main():
         ctx.count(False)
     must = counts.get(kind, {}).get("bytes")
     must_per_launch = must * args.steps / max(cnt, 1) if must else None
-    traffic, traffic_note = traffic_for(kernel, graph_key)
+    traffic, traffic_note = traffic_for(kernel, graph_key, must_per_launch, 1 if args.width <= 32 else 2)
     if must_per_launch:
         achieved = must_per_launch / avg_s / 1e9
         basis = ("bytes the kernel must move, counted on the device by its counting build over "
@@ -602,13 +616,39 @@ def main():
         plain = {"value": plain_te / plain_t, "unit": "TE/s", "pivots": k_plain,
                  "speedup_of_value": value / world / (plain_te / plain_t)}
 
+    # the same workload in batches of 64 (one 64-pivot pass per batch): a
+    # different pivot sequence under the dynamic heuristics (the bc they sample
+    # from is refreshed per batch), so beside the headline, not in it
+    wide = None
+    if not args.skip_wide and args.width == 32:
+        def step64():
+            return ctx.run_sampled(z=args.z, nbfs=args.pivots, bader_c=0, nchecks=1, H=0, seed=seed, W=64)
+        step64()
+        ctx.profile(True)
+        torch.cuda.synchronize()
+        ev4, ev5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev4.record(stream)
+        te64 = 0
+        for _ in range(args.steps):
+            r64 = step64()
+            te64 += r64["te"]
+        ev5.record(stream)
+        torch.cuda.synchronize()
+        prof64 = ctx.profile_read()
+        ctx.profile(False)
+        t64 = ev4.elapsed_time(ev5) / 1000.0
+        wide = {"value": te64 / t64, "unit": "TE/s", "batch_width": 64,
+                "ms_per_step": t64 * 1000 / args.steps, "te_per_step": te64 / args.steps,
+                "pivots_applied_per_step": int(r64["nrounds"]),
+                "kernel_ms": {k: round(v[0], 3) for k, v in prof64.items() if v[1]}}
+
     out = {"metric": metric, "value": value, "unit": "TE/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000 / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "u32 path counts, f32 dependencies/bc",
                "data": "synthetic: the Graph500 generator's graph (seeds 23/24), generated on the device",
            "config": config, "e2e": e2e, "roofline": roofline, "clocks": clk,
-           "gpu_launches": int(launches), "plain_form": plain,
+           "gpu_launches": int(launches), "plain_form": plain, "width_64": wide,
            "te_per_step": te_all / args.steps, "pivots_applied_per_step": int(last["nrounds"])}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

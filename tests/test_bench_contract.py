@@ -17,7 +17,7 @@ def test_defaults(monkeypatch):
     bench, a = _parse(monkeypatch)
     assert a.gpus == 1 and a.warmup >= 3 and a.steps >= 1
     assert a.impl == "gb300" and a.workload == "headline"
-    assert a.scale == 23 and a.edgefactor == 16 and a.pivots == 1024 and a.width == 64 and a.z == 3
+    assert a.scale == 23 and a.edgefactor == 16 and a.pivots == 1024 and a.width == 32 and a.z == 3
 
 
 def test_reference_arm_and_workloads(monkeypatch):
