@@ -176,8 +176,12 @@ struct GridSync {
 // batches of at most AXBC_PERSIST_AUTO_WIDTH pivots on graphs whose last batch
 // was deeper than AXBC_PERSIST_AUTO_LEVELS run their levels in one persistent
 // launch
+#ifndef AXBC_PERSIST_AUTO_LEVELS
 #define AXBC_PERSIST_AUTO_LEVELS 64
-#define AXBC_PERSIST_AUTO_WIDTH 4
+#endif
+#ifndef AXBC_PERSIST_AUTO_WIDTH
+#define AXBC_PERSIST_AUTO_WIDTH 8
+#endif
 
 // Kernel kinds timed by the profiling hooks (axbc_ctx_profile).
 enum {

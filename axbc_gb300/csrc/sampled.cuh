@@ -29,7 +29,9 @@ int sr_begin(axbc_ctx *c, SampledRun *r);
 int sr_draw(axbc_ctx *c, SampledRun *r);
 int sr_nb(const SampledRun *r);
 bool sr_finished(const SampledRun *r);
-int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0);
-int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0);
+// a pass of the drawn pivots [off, off + cnt) of the run's round in lanes
+// lane0.. (cnt is capped by the round and the lanes left)
+int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt = AXBC_WMAX);
+int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt = AXBC_WMAX);
 int sr_result(axbc_ctx *c, SampledRun *r, axbc_run_result *res, std::vector<uint32_t> *piv,
               std::vector<double> *probs, std::vector<uint32_t> *checks);

@@ -550,17 +550,17 @@ __global__ void __launch_bounds__(SAMPLER_TPB) k_sampler(SamplerState *ss, Sampl
 
 // Pivots [off, off + count) of a drawn round become lanes lane0 + 0.. of one
 // pass (count = min(nb - off, AXBC_WMAX - lane0)).
-__global__ void k_load_pass(const SamplerState *ss, BatchInfo *bi, int off, int lane0)
+__global__ void k_load_pass(const SamplerState *ss, BatchInfo *bi, int off, int lane0, int cnt)
 {
     const int s = threadIdx.x;
-    const int count = min(ss->nb - off, AXBC_WMAX - lane0);
+    const int count = min(min(ss->nb - off, AXBC_WMAX - lane0), cnt);
     if (s < count) {
         bi->root[lane0 + s] = ss->v0[off + s];
         bi->p[lane0 + s] = ss->p[off + s];
     }
 }
 
-// After a pass (the drawn pivots [off, off + AXBC_WMAX)): replay Bader's test
+// After a pass (the drawn pivots [off, off + cnt)): replay Bader's test
 // between its pivots, fix how many are applied, and account rounds, skips and
 // traversed edges.  The pass that ends the round also settles the degree-0
 // draws after its last pivot.
@@ -568,10 +568,10 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
                                const float *__restrict__ mdelta, const uint32_t *__restrict__ seen,
                                const uint32_t *__restrict__ reach, const uint32_t *__restrict__ checks,
                                float *b, uint32_t *hist_v, double *hist_p, uint64_t hist_cap,
-                               int off, int lane0, int K)
+                               int off, int lane0, int cnt, int K)
 {
     if (ss->done && ss->nb == 0) return;
-    const int nb = max(0, min(ss->nb - off, AXBC_WMAX - lane0));
+    const int nb = max(0, min(min(ss->nb - off, AXBC_WMAX - lane0), cnt));
     const bool last = off + nb >= ss->nb;
     const uint64_t N = ss->N;
     const uint32_t c = ss->bader_c;
@@ -839,20 +839,32 @@ bool sr_finished(const SampledRun *r)
     return r->ss_host->done && r->ss_host->nb == 0 && r->ss_host->skipped_run == 0;
 }
 
-int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0)
+// Bader's test between two passes of one round, before the next pivot is
+// traversed: the replay's test at that pivot (stop there, nothing applied).
+__global__ void k_sampler_stop_test(SamplerState *ss, const float *__restrict__ bc,
+                                    const uint32_t *__restrict__ checks)
 {
-    k_load_pass<<<1, AXBC_WMAX, 0, c->stream>>>(r->ss, c->bi, off, lane0);
+    if (ss->done || ss->bader_c == 0) return;
+    if (d_bader(bc, checks, ss->nchecks, ss->N, ss->bader_c)) {
+        ss->stopped = 1;
+        ss->done = 1;
+    }
+}
+
+int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt)
+{
+    k_load_pass<<<1, AXBC_WMAX, 0, c->stream>>>(r->ss, c->bi, off, lane0, cnt);
     CU_LAUNCH("k_load_pass");
     return AXBC_OK;
 }
 
-int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0)
+int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt)
 {
     {
         ProfScope ps(c, KP_SAMPLER, 0);
         k_sampler_post<<<1, 1, 0, c->stream>>>(r->ss, c->bi, r->bc, c->mdelta, c->seen, c->g->reach,
                                                r->checks, r->checkval, r->hist_v, r->hist_p,
-                                               r->hist_cap, off, lane0, c->last_batch_k);
+                                               r->hist_cap, off, lane0, cnt, c->last_batch_k);
     }
     CU_LAUNCH("k_sampler_post");
     return AXBC_OK;
@@ -922,33 +934,48 @@ static int ensure_sampler(axbc_ctx *c, uint32_t nchecks)
 }
 
 // One drawn round of one run: its pivots in one pass (widths up to 64); the
-// Bader replay between the pass's pivots decides how many are applied.
+// Bader replay between the pass's pivots decides how many are applied.  The
+// first round of a run with Bader's stop goes in passes of 1, 1, 2, 4, ...
+// pivots instead: with no bc yet the stop may come after any of its pivots,
+// and the pivots of a pass past the stop are traversed for nothing.  Passes
+// split a round without changing it: its pivots were all drawn before it, and
+// each vertex's bc gets their terms in the same order.
 static int sr_round_alone(axbc_ctx *c, SampledRun *r)
 {
     const int nb = sr_nb(r);
-    for (int off = 0; off == 0 || off < nb; off += AXBC_WMAX) {
-        const int cnt = std::min(nb - off, AXBC_WMAX);
+    const bool ramp = r->prm.bader_c > 0 && r->batches == 0;
+    int want = ramp ? 1 : AXBC_WMAX;
+    for (int off = 0; off == 0 || off < nb;) {
+        const int cnt = std::min(nb - off, want);
         if (cnt > 0) {
-            TRY(sr_load(c, r, off, 0));
+            TRY(sr_load(c, r, off, 0, cnt));
             TRY(axbc_batch_traverse(c, cnt, r->prm.H));
             r->batches++;
             float *tg[AXBC_WMAX];
             for (int i = 0; i < AXBC_WMAX; i++) tg[i] = r->bc;
             TRY(axbc_batch_set_targets(c, tg));
         }
-        TRY(sr_post(c, r, off, 0));
+        TRY(sr_post(c, r, off, 0, std::max(cnt, 0)));
         if (cnt > 0) {
             float *dout[1] = {r->delta_last};
             const int lo[1] = {0}, hi[1] = {AXBC_WMAX};
             TRY(axbc_batch_apply_lanes(c, dout, lo, hi, 1));
         }
-        if (off + AXBC_WMAX < nb) {
-            // a later pass runs only if Bader's test did not stop the round
+        if (off + cnt < nb) {
+            // a later pass runs only if Bader's test did not stop the round,
+            // at or before its first pivot
+            {
+                ProfScope ps(c, KP_SAMPLER, 0);
+                k_sampler_stop_test<<<1, 1, 0, c->stream>>>(r->ss, r->bc, r->checks);
+            }
+            CU_LAUNCH("k_sampler_stop_test");
             CU(cudaMemcpyAsync(&r->ss_host->done, &r->ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                c->stream));
             CU(cudaStreamSynchronize(c->stream));
             if (r->ss_host->done) break;
         }
+        off += std::max(cnt, 1);
+        if (ramp && off > 1) want = std::min(2 * want, AXBC_WMAX);
     }
     return AXBC_OK;
 }

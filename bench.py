@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--skip-serving", action="store_true", help="no serving phase after the headline")
     ap.add_argument("--skip-count", action="store_true", help="no counted step (roofline bytes)")
     ap.add_argument("--skip-wide", action="store_true", help="no width-64 leg after the headline")
+    ap.add_argument("--persistent", default="auto", choices=["auto", "on", "off"],
+                    help="level loop: one cooperative launch per pass (on), per-level launches (off), "
+                         "or the library's rule (auto: narrow batches on deep graphs)")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "serving", "config1", "config2", "config3"],
                     help="serving: the request server on resident graphs (p50/p99 latency); "
@@ -230,6 +233,10 @@ CONFIGS = {
 }
 
 
+# --persistent: the library's level-loop modes (axbc_set_persistent)
+PERSIST_MODES = {"off": -1, "auto": 0, "on": 1}
+
+
 def config_bench(args):
     """One of the other benchmark configurations: each step is one whole
     sampled run on the GPU (CUDA events on the context's stream); the oracle
@@ -247,6 +254,7 @@ def config_bench(args):
     build_s = time.perf_counter() - t_graph
     stream = torch.cuda.Stream()
     ctx = ax.Context(G, stream=stream.cuda_stream)
+    ctx.set_persistent(PERSIST_MODES[args.persistent])
     W = cf["W"]
     if W is None:
         deg = G.deg()
@@ -275,7 +283,7 @@ def config_bench(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000 / args.steps,
            "higher_is_better": True, "impl": "gb300", "workload": args.workload,
            "config": {"workload": cf["desc"], "batch_width": W, "graph_build_s": round(build_s, 3),
-                      "n": G.n, "m": G.m},
+                      "n": G.n, "m": G.m, "level_loop": args.persistent},
            "rounds": int(r["nrounds"]), "stopped": bool(r["stopped"]), "te_per_run": int(r["te"])}
     if not args.no_cpu_baseline:
         col, row, reach = G.csc()
@@ -422,6 +430,8 @@ def main():
                        "build_s": round(time.perf_counter() - t_graph, 3)}
     stream = torch.cuda.Stream()
     ctx = ax.Context(G, stream=stream.cuda_stream)
+    ctx.set_persistent(PERSIST_MODES[args.persistent])
+    config["level_loop"] = args.persistent
 
     def step(seed):
         return ctx.run_sampled(z=args.z, nbfs=args.pivots, bader_c=0, nchecks=1, H=0, seed=seed,

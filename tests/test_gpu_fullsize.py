@@ -2,8 +2,8 @@
 bit against the oracle on a bounded number of pivots.
 
 - Headline (Kronecker scale 23, the Graph500 generator with seeds 23/24,
-  undirected, -z 3, batches of 32): three passes of the bench's own sampled
-  run.  With n = 2^23 the reference's `int LIMxSAMPLE = N*N` truncates to 0
+  undirected, -z 3, batches of 32, and of 64 as in the bench's width-64 leg):
+  passes of the bench's own sampled run.  With n = 2^23 the reference's `int LIMxSAMPLE = N*N` truncates to 0
   (src/axbc2d.c:2835), so the first draw of an already-used pivot drops its
   round (:2876, 3072-3077); this run must hit that path.
 - Serving: requests on the resident serving graphs (Kronecker scales 20 and 22
@@ -23,23 +23,29 @@ def same_bits(got, want, what):
     assert same.all(), f"{what}: {np.count_nonzero(~same)} of {len(got)} values differ"
 
 
-def test_headline_scale23_sampled_run(axbc, orc):
+@pytest.fixture(scope="module")
+def scale23(axbc, orc):
     G = axbc.Graph.kronecker(23, 16, 23, 24)
     assert G.n == 1 << 23 and G.m == 259289870
-    ctx = axbc.Context(G)
-    got = ctx.run_sampled(z=3, nbfs=96, bader_c=0, nchecks=1, H=0, seed=4343543, W=32)
-    bc = ctx.bc()
     col, row, reach = G.csc()
-    g = orc.CSC(col, row, reach)
-    want = orc.run(g, z=3, nbfs=96, bader_c=0, nchecks=1, H=0, seed=4343543, W=32)
+    return G, orc.CSC(col, row, reach)
+
+
+@pytest.mark.parametrize("W,nbfs", [(32, 96), (64, 128)])
+def test_headline_scale23_sampled_run(axbc, orc, scale23, W, nbfs):
+    """Three (width 32) or two (width 64) passes of the headline's sampled run."""
+    G, g = scale23
+    ctx = axbc.Context(G)
+    got = ctx.run_sampled(z=3, nbfs=nbfs, bader_c=0, nchecks=1, H=0, seed=4343543, W=W)
+    bc = ctx.bc()
+    want = orc.run(g, z=3, nbfs=nbfs, bader_c=0, nchecks=1, H=0, seed=4343543, W=W)
     assert want["dropped"] > 0, "no round dropped by the truncated bad-sample limit"
     for k in ("nrounds", "skipped", "dropped", "ui_end", "te"):
         assert got[k] == want[k], k
     assert np.array_equal(got["pivots"], want["pivots"])
     assert np.array_equal(got["probs"], want["probs"])
-    same_bits(bc, want["bc"], "scale-23 bc")
+    same_bits(bc, want["bc"], f"scale-23 bc, width {W}")
     ctx.close()
-    G.close()
 
 
 # (graph, z, nbfs, bader_c, nchecks, seed, W)

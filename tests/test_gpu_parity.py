@@ -184,6 +184,34 @@ def test_bader_stop_matches_oracle(axbc, orc, W):
         assert_float_exact(ctx.bc(), want["bc"], "bc")
 
 
+@pytest.mark.parametrize("W", [16, 64])
+def test_bader_first_round_in_growing_passes(axbc, orc, W):
+    """A run with Bader's stop traverses its first drawn round in passes of 1,
+    1, 2, 4, ... pivots, testing the stop between passes before traversing on:
+    the same pivots, counters and bits as the oracle's run at that width, and
+    when the stop comes inside the first round, only the passes up to it."""
+    G = axbc.Graph.grid(128, 0.02, 1e-3, seed=5)
+    col, row, reach = G.csc()
+    g = orc.CSC(col, row, reach)
+    for z, c, x, seed in ((4, 1, 4, 7), (0, 1, 2, 3), (3, 2, 8, 5)):
+        ctx = axbc.Context(G)
+        got = ctx.run_sampled(z=z, nbfs=64, bader_c=c, nchecks=x, seed=seed, W=W)
+        want = orc.run(g, z=z, nbfs=64, bader_c=c, nchecks=x, seed=seed, W=W)
+        what = f"z={z} c={c} x={x} W={W}"
+        assert got["stopped"] == want["stopped"], what
+        for k in ("nrounds", "skipped", "dropped", "ui_end", "te"):
+            assert got[k] == want[k], (what, k)
+        assert np.array_equal(got["pivots"], want["pivots"]), what
+        assert np.array_equal(got["checks"], want["checks"]), what
+        assert_float_exact(ctx.bc(), want["bc"], what)
+        assert_float_exact(ctx.delta(), want["delta_last"], what)
+        k = int(want["nrounds"])
+        if want["stopped"] and k < W:
+            # passes cover 1, 2, 4, ... pivots: the one holding pivot k + 1 is the last
+            assert got["batches"] <= max(1, int(np.ceil(np.log2(k + 1)))) + 1, (what, k, got["batches"])
+        ctx.close()
+
+
 def test_static_distributions(axbc, orc):
     for H in (0, 1):
         g, G = make(axbc, orc, golden_edges(), 1024, True, H)
