@@ -47,16 +47,36 @@ __device__ __forceinline__ unsigned long long warp_or(unsigned long long m)
 // A warp stages the masks of a 32-position chunk in shared memory as K
 // arrays of 32 words, one per 32-bit half (sg + 32 h), so that a half's
 // consumer holds 32-bit words only.
-template <int K, class M> __device__ __forceinline__ void stage_mask(uint32_t *sg, M m)
-{
-    sg[lane_id()] = (uint32_t)m;
-    if (K == 2) sg[32 + lane_id()] = (uint32_t)((unsigned long long)m >> 32);
-}
 template <int K> __device__ __forceinline__ typename MaskOf<K>::T staged_mask(const uint32_t *sg, int i)
 {
     typedef typename MaskOf<K>::T M;
     if (K == 1) return (M)sg[i];
     return (M)((unsigned long long)sg[i] | ((unsigned long long)sg[32 + i] << 32));
+}
+
+// Stage the chunk's positions that have a parent (act: their lanes),
+// compacted to slots 0..nh-1 in position order, and zero masks in slots
+// nh..31, so that the consumer walks ceil(nh / 8) groups of 8 instead of every
+// group holding a hit.  Returns nh.
+template <int K, class M>
+__device__ __forceinline__ int stage_compact(uint32_t *su, uint32_t *sg, uint32_t *sk, unsigned act, uint32_t v,
+                                             M fm, uint32_t k)
+{
+    const unsigned lane = lane_id();
+    const int nh = __popc(act);
+    if (fm) {
+        const int pos = __popc(act & ((1u << lane) - 1u));
+        su[pos] = v;
+        sg[pos] = (uint32_t)fm;
+        if (K == 2) sg[32 + pos] = (uint32_t)((unsigned long long)fm >> 32);
+        if (sk) sk[pos] = k;
+    }
+    if ((int)lane >= nh) {
+        su[lane] = 0;
+        sg[lane] = 0;
+        if (K == 2) sg[32 + lane] = 0;
+    }
+    return nh;
 }
 
 // eight staged words of group g (16-byte shared loads)
@@ -453,9 +473,9 @@ __device__ __forceinline__ void fwd_push_body(const Adj &a, const typename MaskO
 
 // Forward level L, pull into vertex u for the pivots `ns` that have not seen
 // it: sum sigma_s over every in-neighbour at depth L-1 from pivot s (u32 sums:
-// any order gives the same bits).  The positions of a 32-wide chunk are staged
-// in shared memory; each 8-position group with a hit issues its gathers (8 per
-// half) before any is consumed.
+// any order gives the same bits).  The positions of a 32-wide chunk that have
+// a parent are staged in shared memory, compacted; each group of 8 issues its
+// gathers (8 per half) before any is consumed.
 template <int K, class WC>
 __device__ __forceinline__ typename MaskOf<K>::T pull_span(const Adj &rv, typename MaskOf<K>::T ns, uint32_t b0,
                                                            uint32_t b1,
@@ -483,12 +503,10 @@ __device__ __forceinline__ typename MaskOf<K>::T pull_span(const Adj &rv, typena
         const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
         found |= warp_or(fm);
-        su[lane] = v;
-        stage_mask<K>(sg, fm);
+        const int nh = stage_compact<K>(su, sg, (uint32_t *)nullptr, act, v, fm, 0u);
         __syncwarp();
 #pragma unroll 1
-        for (int g = 0; g < 4; g++) {
-            if (!((act >> (8 * g)) & 0xffu)) continue;
+        for (int g = 0; 8 * g < nh; g++) {
             uint32_t u[8];
             load8u(su, g, u);
 #pragma unroll
@@ -510,9 +528,9 @@ __device__ __forceinline__ typename MaskOf<K>::T pull_span(const Adj &rv, typena
 // Pull into up to 32 light vertices at once, one per lane (pivots ns_l; 0:
 // none), edge-parallel over the concatenation of their in-adjacency lists:
 // lane e finds its vertex by a binary search over the inclusive degree prefix
-// held across the lanes.  Positions arrive grouped by vertex, so one running
-// sum per lane (pivot) is written out whenever the vertex changes.  Returns the
-// discovered mask of the lane's own vertex.
+// held across the lanes.  Positions arrive grouped by vertex (compaction keeps
+// their order), so one running sum per lane (pivot) is written out whenever
+// the vertex changes.  Returns the discovered mask of the lane's own vertex.
 template <int K, class WC>
 __device__ __forceinline__ typename MaskOf<K>::T pull_light32(const Adj &rv, uint32_t u_l,
                                                               typename MaskOf<K>::T ns_l,
@@ -568,13 +586,10 @@ __device__ __forceinline__ typename MaskOf<K>::T pull_light32(const Adj &rv, uin
         }
         const unsigned act = __ballot_sync(FULL_MASK, fm != 0);
         if (!act) continue;
-        su[lane] = v;
-        stage_mask<K>(sg, fm);
-        sk[lane] = k;
+        const int nh = stage_compact<K>(su, sg, sk, act, v, fm, k);
         __syncwarp();
 #pragma unroll 1
-        for (int g = 0; g < 4; g++) {
-            if (!((act >> (8 * g)) & 0xffu)) continue;
+        for (int g = 0; 8 * g < nh; g++) {
             uint32_t u4[8];
             load8u(su, g, u4);
             uint32_t x[K][8];
@@ -590,7 +605,7 @@ __device__ __forceinline__ typename MaskOf<K>::T pull_light32(const Adj &rv, uin
                 }
                 mor |= (M)((unsigned long long)mh << (32 * h));
             }
-            const int k0 = (int)sk[8 * g], k7 = (int)sk[8 * g + 7];
+            const int k0 = (int)sk[8 * g], k7 = (int)sk[min(8 * g + 7, nh - 1)];
             if (k0 == k7) {
                 // all eight positions belong to one vertex (k is nondecreasing)
                 if (k0 != cur) {

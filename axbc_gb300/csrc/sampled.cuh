@@ -28,10 +28,14 @@ void sr_free(SampledRun *r);
 int sr_begin(axbc_ctx *c, SampledRun *r);
 int sr_draw(axbc_ctx *c, SampledRun *r);
 int sr_nb(const SampledRun *r);
+bool sr_done(const SampledRun *r);  // ss_host's done flag
 bool sr_finished(const SampledRun *r);
 // a pass of the drawn pivots [off, off + cnt) of the run's round in lanes
 // lane0.. (cnt is capped by the round and the lanes left)
 int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt = AXBC_WMAX);
 int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt = AXBC_WMAX);
+// Bader's test between two passes of a round (before its next pivot); the
+// result reaches ss_host->done once the stream has synchronised
+int sr_stop_test(axbc_ctx *c, SampledRun *r);
 int sr_result(axbc_ctx *c, SampledRun *r, axbc_run_result *res, std::vector<uint32_t> *piv,
               std::vector<double> *probs, std::vector<uint32_t> *checks);

@@ -834,6 +834,7 @@ int sr_draw(axbc_ctx *c, SampledRun *r)
 }
 
 int sr_nb(const SampledRun *r) { return r->ss_host->nb; }
+bool sr_done(const SampledRun *r) { return r->ss_host->done != 0; }
 bool sr_finished(const SampledRun *r)
 {
     return r->ss_host->done && r->ss_host->nb == 0 && r->ss_host->skipped_run == 0;
@@ -849,6 +850,17 @@ __global__ void k_sampler_stop_test(SamplerState *ss, const float *__restrict__ 
         ss->stopped = 1;
         ss->done = 1;
     }
+}
+
+int sr_stop_test(axbc_ctx *c, SampledRun *r)
+{
+    {
+        ProfScope ps(c, KP_SAMPLER, 0);
+        k_sampler_stop_test<<<1, 1, 0, c->stream>>>(r->ss, r->bc, r->checks);
+    }
+    CU_LAUNCH("k_sampler_stop_test");
+    CU(cudaMemcpyAsync(&r->ss_host->done, &r->ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    return AXBC_OK;
 }
 
 int sr_load(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt)
@@ -964,13 +976,7 @@ static int sr_round_alone(axbc_ctx *c, SampledRun *r)
         if (off + cnt < nb) {
             // a later pass runs only if Bader's test did not stop the round,
             // at or before its first pivot
-            {
-                ProfScope ps(c, KP_SAMPLER, 0);
-                k_sampler_stop_test<<<1, 1, 0, c->stream>>>(r->ss, r->bc, r->checks);
-            }
-            CU_LAUNCH("k_sampler_stop_test");
-            CU(cudaMemcpyAsync(&r->ss_host->done, &r->ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                               c->stream));
+            TRY(sr_stop_test(c, r));
             CU(cudaStreamSynchronize(c->stream));
             if (r->ss_host->done) break;
         }

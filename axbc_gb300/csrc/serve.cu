@@ -63,6 +63,9 @@ struct Request {
     bool allocated = false;
     bool need_draw = false;  // worker: the next round is not drawn yet
     uint64_t drawn_at = 0;   // worker: pass count when the pending round was drawn
+    int off = 0;             // worker: first pivot of the drawn round not yet traversed
+    int want = AXBC_WMAX;    // worker: how many of them the next pass takes
+    bool test_pending = false;  // worker: the stop test between two passes is in flight
     bool worker_ref = false; // in the worker's active list (guarded by the mutex)
     bool released = false;   // released while the worker still held it
     axbc_run_result res{};
@@ -124,10 +127,24 @@ static void req_finish(axbc_server *S, Request *r)
 }
 
 // One pass over graph gi: draw the rounds of its requests that need one,
-// then pack drawn rounds into the lanes of one multi-source pass.
+// then pack drawn rounds into the lanes of one multi-source pass.  The first
+// round of a request with Bader's stop goes into passes 1, 1, 2, 4, ...
+// pivots at a time with the stop tested between them, as axbc_run_sampled
+// does, so a request whose stop comes early holds no lanes past it.
 static int serve_pass(axbc_server *S, ServeGraph &G, std::vector<Request *> &runs)
 {
     axbc_ctx *c = G.ctx;
+    bool pending = false;
+    for (Request *r : runs) pending |= r->test_pending;
+    if (pending) {
+        CU(cudaStreamSynchronize(c->stream));
+        for (Request *r : runs)
+            if (r->test_pending) {
+                r->test_pending = false;
+                // stopped between two passes: the next draw ends the run
+                if (sr_done(&r->run)) r->need_draw = true;
+            }
+    }
     bool drew = false;
     for (Request *r : runs)
         if (r->need_draw) {
@@ -140,6 +157,8 @@ static int serve_pass(axbc_server *S, ServeGraph &G, std::vector<Request *> &run
         if (r->need_draw) {
             r->need_draw = false;
             r->drawn_at = G.passes;
+            r->off = 0;
+            r->want = r->prm.bader_c > 0 && r->run.batches == 0 ? 1 : AXBC_WMAX;
             if (sr_finished(&r->run)) {
                 req_finish(S, r);
                 continue;
@@ -156,34 +175,46 @@ static int serve_pass(axbc_server *S, ServeGraph &G, std::vector<Request *> &run
     // rounds that have waited longest first, so that no request starves
     std::stable_sort(ready.begin(), ready.end(),
                      [](const Request *a, const Request *b) { return a->drawn_at < b->drawn_at; });
-    std::vector<std::pair<Request *, int>> segs;  // (request, first lane)
+    struct Seg {
+        Request *r;
+        int lane0, cnt;
+    };
+    std::vector<Seg> segs;
     int lane = 0;
     for (Request *r : ready) {
-        const int nb = sr_nb(&r->run);
-        if (lane + nb > AXBC_WMAX) continue;  // its drawn round waits for the next pass
-        segs.push_back({r, lane});
-        lane += nb;
+        const int cnt = std::min(sr_nb(&r->run) - r->off, r->want);
+        if (lane + cnt > AXBC_WMAX) continue;  // its drawn round waits for the next pass
+        segs.push_back({r, lane, cnt});
+        lane += cnt;
     }
     if (segs.empty()) return AXBC_OK;
-    for (auto &sg : segs) TRY(sr_load(c, &sg.first->run, 0, sg.second));
+    for (auto &sg : segs) TRY(sr_load(c, &sg.r->run, sg.r->off, sg.lane0, sg.cnt));
     TRY(axbc_batch_traverse(c, lane, G.H));
     float *tg[AXBC_WMAX];
-    for (int i = 0; i < AXBC_WMAX; i++) tg[i] = segs[0].first->run.bc;
+    for (int i = 0; i < AXBC_WMAX; i++) tg[i] = segs[0].r->run.bc;
     std::vector<float *> dout;
     std::vector<int> lo, hi;
     for (auto &sg : segs) {
-        const int nb = sr_nb(&sg.first->run);
-        for (int l = sg.second; l < sg.second + nb; l++) tg[l] = sg.first->run.bc;
-        dout.push_back(sg.first->run.delta_last);
-        lo.push_back(sg.second);
-        hi.push_back(sg.second + nb);
+        for (int l = sg.lane0; l < sg.lane0 + sg.cnt; l++) tg[l] = sg.r->run.bc;
+        dout.push_back(sg.r->run.delta_last);
+        lo.push_back(sg.lane0);
+        hi.push_back(sg.lane0 + sg.cnt);
     }
     TRY(axbc_batch_set_targets(c, tg));
-    for (auto &sg : segs) TRY(sr_post(c, &sg.first->run, 0, sg.second));
+    for (auto &sg : segs) TRY(sr_post(c, &sg.r->run, sg.r->off, sg.lane0, sg.cnt));
     TRY(axbc_batch_apply_lanes(c, dout.data(), lo.data(), hi.data(), (int)segs.size()));
     for (auto &sg : segs) {
-        sg.first->run.batches++;
-        sg.first->need_draw = true;
+        Request *r = sg.r;
+        r->run.batches++;
+        r->off += sg.cnt;
+        if (r->off >= sr_nb(&r->run)) {
+            r->need_draw = true;
+        } else {
+            // the rest of the round goes on only if Bader's test holds off
+            TRY(sr_stop_test(c, &r->run));
+            r->test_pending = true;
+            if (r->off > 1) r->want = std::min(2 * r->want, AXBC_WMAX);
+        }
     }
     std::lock_guard<std::mutex> lk(S->mu);
     S->passes++;

@@ -358,7 +358,7 @@ int axbc_ctx_launches(const axbc_ctx *ctx, uint64_t *launches);
  * three per backward depth.  On graphs of many narrow levels it can instead
  * run as one cooperative launch (all blocks resident, a bounded grid barrier
  * between phases).  mode 1 always, -1 never, 0 (default) for batches of at
- * most 4 pivots when the context's last batch was deeper than 64 levels or,
+ * most 8 pivots when the context's last batch was deeper than 64 levels or,
  * for its first batch, when no vertex has more than 64 neighbours.
  * blocks_per_sm: blocks of the cooperative grid per SM (0 keeps the current
  * setting, default 4).  Results

@@ -33,13 +33,15 @@ def scale23(axbc, orc):
 
 @pytest.mark.parametrize("W,nbfs", [(32, 96), (64, 128)])
 def test_headline_scale23_sampled_run(axbc, orc, scale23, W, nbfs):
-    """Three (width 32) or two (width 64) passes of the headline's sampled run."""
+    """Three (width 32) or two (width 64) passes of the headline's sampled run;
+    the width-32 run hits rounds dropped by the truncated bad-sample limit."""
     G, g = scale23
     ctx = axbc.Context(G)
     got = ctx.run_sampled(z=3, nbfs=nbfs, bader_c=0, nchecks=1, H=0, seed=4343543, W=W)
     bc = ctx.bc()
     want = orc.run(g, z=3, nbfs=nbfs, bader_c=0, nchecks=1, H=0, seed=4343543, W=W)
-    assert want["dropped"] > 0, "no round dropped by the truncated bad-sample limit"
+    if W == 32:
+        assert want["dropped"] > 0, "no round dropped by the truncated bad-sample limit"
     for k in ("nrounds", "skipped", "dropped", "ui_end", "te"):
         assert got[k] == want[k], k
     assert np.array_equal(got["pivots"], want["pivots"])
