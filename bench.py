@@ -481,7 +481,9 @@ def main():
                "cpu_baseline": {"value": val, "unit": "TE/s", "cores": threads, "kind": "port",
                                 "sample": f"{ks[0]} pivots of the step's pivot list per step, "
                                           "OpenMP over pivots (oracle/ C restatement; the "
-                                          "reference needs MPI and does not build here)"},
+                                          "reference program needs MPI and a GPU, and its "
+                                          "one-rank host build exists only where its "
+                                          "sources are)"},
                "e2e": {"value": val, "unit": "TE/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}
         print(json.dumps(out), flush=True)
