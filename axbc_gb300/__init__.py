@@ -520,7 +520,7 @@ def srand48(seed):
 class Server:
     """Request server over resident graphs (axbc_server_* / axbc_request_*).
 
-    Requests are sampled runs (run_sampled's parameters, W <= 32); the server
+    Requests are sampled runs (run_sampled's parameters, W <= 64); the server
     batches the rounds of concurrent requests on one graph into shared passes.
     """
 

@@ -1,11 +1,12 @@
-// Batched form: up to 32 pivots in one multi-source pass.  Lane s of a warp
-// owns pivot s; every vertex carries one 32-bit mask per BFS level (bit s:
-// the vertex is at that depth from pivot s), a `seen` mask, and per-pivot path
-// counts / dependencies laid out [vertex][32] so the 32 lanes touch one
-// 128-byte line.  Results equal those of the plain form bit for bit: path
-// counts are integers, and each lane accumulates its dependency sum in the
-// canonical order (32-position chunks summed as a tree in registers, chunks
-// then spans left to right).
+// Batched form: up to 64 pivots in one multi-source pass.  Lane s of a warp
+// owns pivot s (and s + 32 in a pass of more than 32); every vertex carries one
+// 32- or 64-bit mask per BFS level (bit s: the vertex is at that depth from
+// pivot s), a `seen` mask, and per-pivot path counts / dependencies laid out
+// [vertex][32 or 64] so a warp touches one 128-byte line per 32 pivots.
+// Results equal those of the plain form bit for bit: path counts are integers,
+// and each lane accumulates its dependency sum in the canonical order
+// (32-position chunks summed as a tree in registers, chunks then spans left to
+// right).
 #include <algorithm>
 #include <cstddef>
 #include <vector>
@@ -1974,9 +1975,10 @@ template <int K> static int traverse_stepwise(axbc_ctx *c, int nsrc, int sgrid, 
 // context says so; otherwise for a batch of at most AXBC_PERSIST_AUTO_WIDTH
 // pivots when the last batch was deep, or -- for the first batch -- when no
 // vertex has more than 64 neighbours (meshes and road-like graphs, whose many
-// levels are narrow).  Measured on 1024^2 and 2048^2 grids: one pivot 14.0 ->
-// 9.9 ms and 19.1 -> 15.8 ms per pass; at 8 pivots even, at 32 pivots the
-// step kernels' fuller grids win.  Counting runs use the step kernels.
+// levels are narrow).  Measured on the 1024^2 grid (wall clock, 32 pivots per
+// run): width 1 41.8 -> 32.8 ms, width 4 32.2 -> 26.0, width 8 34.3 -> 30.2,
+// width 16 42.1 -> 40.2, width 32 even; on shallow graphs the step kernels'
+// fuller grids win.  Counting runs use the step kernels.
 static bool use_persist(axbc_ctx *c, int nsrc)
 {
     if (c->count_on || c->persist_mode < 0) return false;

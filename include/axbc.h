@@ -154,7 +154,7 @@ int axbc_ctx_set_tuning(axbc_ctx *ctx, double push_factor_single, double push_fa
 typedef struct {
     double push_factor_single;
     double push_factor_batch;
-    int32_t batch_width;       /* fastest width <= 32 on these pivots */
+    int32_t batch_width;       /* fastest width <= AXBC_MAX_BATCH on these pivots */
     int32_t pad;
     double batch_te_per_s;     /* best trial rates */
     double plain_te_per_s;
