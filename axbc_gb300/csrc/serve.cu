@@ -27,6 +27,11 @@
 #include "common.cuh"
 #include "sampled.cuh"
 
+// pivots per round of the requests whose width does not change their bits
+#ifndef AXBC_SERVE_STATIC_WIDTH
+#define AXBC_SERVE_STATIC_WIDTH AXBC_W
+#endif
+
 namespace {
 
 uint64_t now_ns()
@@ -266,7 +271,7 @@ static void serve_graph_loop(axbc_server *S, int gi)
             // where a round ends) the width only sets how many pivots share a
             // pass: run them 32 wide (same pivots, bits and counters)
             axbc_run_params prm = r->prm;
-            if (prm.z <= 2 && prm.bader_c == 0) prm.batch_width = AXBC_W;
+            if (prm.z <= 2 && prm.bader_c == 0) prm.batch_width = AXBC_SERVE_STATIC_WIDTH;
             int st = sr_alloc(G.g, &prm, &r->run);
             if (st == AXBC_OK) {
                 r->allocated = true;
@@ -353,6 +358,13 @@ extern "C" int axbc_server_add_graph(axbc_server *S, axbc_graph *g, int H, int *
     CU(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
     int st = axbc_ctx_create(g, G->stream, &G->ctx);
     if (st == AXBC_OK) st = axbc_ensure_batch(G->ctx);
+    // the static sampling distributions (degrees, LCC) of the resident graph
+    // are built now, not by the first request that needs them: their
+    // triangle count can hold the device for a while on a large graph
+    if (st == AXBC_OK) st = axbc_build_deg_dist(g, G->stream);
+    if (st == AXBC_OK) st = axbc_build_lcc(g, G->stream);
+    if (st == AXBC_OK && cudaStreamSynchronize(G->stream) != cudaSuccess)
+        st = axbc_cuda_fail(cudaGetLastError(), "server graph set-up", __FILE__, __LINE__);
     if (st != AXBC_OK) {
         if (G->ctx) axbc_ctx_destroy(G->ctx);
         cudaStreamDestroy(G->stream);

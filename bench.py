@@ -377,6 +377,11 @@ def serve_bench(args, emit=True):
            "span_s": span, "passes": st["passes"], "lanes_per_pass": st["lanes"] / max(1, st["passes"]),
            "p50_by_graph_s": {k: float(np.median(v)) for k, v in per_graph.items()},
            "worker_by_graph": {graphs[i][0]: srv.graph_stats(g) for i, g in enumerate(gids)},
+           "slowest": [{"graph": graphs[jobs[k][1]][0], "z": jobs[k][2], "N": jobs[k][3], "c": jobs[k][4],
+                        "x": jobs[k][5], "latency_s": round(float(lat[k]), 3),
+                        "queue_wait_s": round(float(wait[k]), 3), "rounds": int(infos[k]["nrounds"]),
+                        "stopped": bool(infos[k]["stopped"])}
+                       for k in np.argsort(-lat)[:3]],
            "dtype": "u32 path counts, f32 dependencies", "data": "synthetic (Graph500 generator, seeds 23/24, on the device; grid)",
            "config": {"workload": "serving: resident kronecker s16/s18/s20/s22 ef16 + grid 1024^2; "
                                   "Poisson arrivals (seed 11); -z 0..5; width 8; -N log-uniform "

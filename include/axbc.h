@@ -287,7 +287,9 @@ typedef struct {
 int axbc_server_create(uint64_t hbm_budget, axbc_server **server);
 /* Make graph g (owned by the caller, alive until the server is destroyed)
  * resident, with its own stream and worker thread; H is the graph's one-degree
- * reduction (requests must match). */
+ * reduction (requests must match).  The graph's static sampling distributions
+ * (degree-based and LCC) are built before the call returns, so that no request
+ * waits for them. */
 int axbc_server_add_graph(axbc_server *server, axbc_graph *g, int H, int *graph_id);
 /* Queue a sampled run; AXBC_ERR_BUSY if it can never fit in the budget. */
 int axbc_request_submit(axbc_server *server, int graph_id, const axbc_run_params *prm,
