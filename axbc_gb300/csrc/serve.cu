@@ -29,7 +29,7 @@
 
 // pivots per round of the requests whose width does not change their bits
 #ifndef AXBC_SERVE_STATIC_WIDTH
-#define AXBC_SERVE_STATIC_WIDTH AXBC_W
+#define AXBC_SERVE_STATIC_WIDTH AXBC_WMAX
 #endif
 
 namespace {
@@ -269,7 +269,7 @@ static void serve_graph_loop(axbc_server *S, int gi)
             // static heuristics (-z 0..2) draw from distributions no pivot
             // changes, so without Bader's stop (whose round counter depends on
             // where a round ends) the width only sets how many pivots share a
-            // pass: run them 32 wide (same pivots, bits and counters)
+            // pass: run them 64 wide (same pivots, bits and counters)
             axbc_run_params prm = r->prm;
             if (prm.z <= 2 && prm.bader_c == 0) prm.batch_width = AXBC_SERVE_STATIC_WIDTH;
             int st = sr_alloc(G.g, &prm, &r->run);

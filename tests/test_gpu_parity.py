@@ -404,7 +404,7 @@ def test_sample_and_stop_primitives_rebuild_the_run(axbc, orc, z):
 def test_static_heuristics_do_not_depend_on_width(axbc, orc, z):
     """With a distribution no pivot changes, the width only groups the same pivot
     sequence into passes: bc bits, pivots and counters are the same at every width
-    (the request server relies on this to run static requests 32 wide).  With
+    (the request server relies on this to run static requests 64 wide).  With
     Bader's stop the applied pivots and bc still agree; only the round counter
     depends on where the stopping round ends."""
     H = 1 if z == 1 else 0
