@@ -77,10 +77,11 @@ def _failure_loop(axbc, G, run, want, name):
 
 
 def test_server_recovers_from_each_failed_allocation(axbc, golden):
-    """A device allocation made to fail at each point of adding a graph and
-    serving a request (the server's worker thread included): the call or the
-    request fails with AXBC_ERR_NOMEM, a second request on the same server gets
-    the exact result, and closing the server frees every byte."""
+    """A device allocation made to fail at each point of adding a graph (its
+    static sampling distributions included) and serving a request (the
+    server's worker thread included): the call or the request fails with
+    AXBC_ERR_NOMEM, a second request on the same server gets the exact result,
+    and closing the server and the graph frees every byte."""
     g, G = golden
     prm = dict(z=3, nbfs=48, bader_c=0, nchecks=1, H=0, seed=9, W=8)
     ref = axbc.Context(G)
@@ -92,12 +93,14 @@ def test_server_recovers_from_each_failed_allocation(axbc, golden):
     try:
         L = axbc.lib()
         base = L.axbc_device_bytes_live()
-        for k in range(40):
+        for k in range(60):
+            # a fresh graph each time: adding it builds its distributions
+            Gk = axbc.Graph.from_csc(g.col, g.row, g.reach)
             srv = axbc.Server()
             L.axbc_inject_alloc_failure_after(k)
             failed = False
             try:
-                gid = srv.add_graph(G, H=0)
+                gid = srv.add_graph(Gk, H=0)
                 info = srv.wait(srv.submit(gid, **prm), timeout_ms=60000)
                 if info["state"] == "failed":
                     assert info["status"] == 3, info
@@ -111,13 +114,14 @@ def test_server_recovers_from_each_failed_allocation(axbc, golden):
             finally:
                 L.axbc_inject_alloc_failure_after(-1)
             if gid is None:
-                gid = srv.add_graph(G, H=0)
+                gid = srv.add_graph(Gk, H=0)
             rid = srv.submit(gid, **prm)
             info = srv.wait(rid, timeout_ms=60000)
             assert info["state"] == "done", (k, info)
-            bc, _, _ = srv.result(rid, G.n)
+            bc, _, _ = srv.result(rid, Gk.n)
             same_bits(bc, want, f"server, failure after {k} allocations")
             srv.close()
+            Gk.close()
             assert L.axbc_device_bytes_live() == base, f"server: leak after failing allocation {k}"
             if not failed:
                 break
