@@ -152,11 +152,18 @@ __global__ void k_batch_init(BatchInfo *bi, int nsrc, int H, float *bc, uint32_t
                              double push_factor, unsigned long long push_min,
                              unsigned long long *level_te,
                              unsigned long long *level_cnt, LevelLists ll, uint32_t pool_cap,
-                             uint32_t list_max)
+                             uint32_t list_max, const uint32_t *__restrict__ to_view)
 {
     typedef typename MaskOf<K>::T M;
     M *fmask0 = reinterpret_cast<M *>(fmask0_), *seen = reinterpret_cast<M *>(seen_);
     const int l = threadIdx.x;
+    // the roots arrive as vertex ids; the pass runs in the graph's view
+    if (to_view) {
+#pragma unroll
+        for (int h = 0; h < K; h++)
+            if (l + 32 * h < nsrc) bi->root[l + 32 * h] = to_view[bi->root[l + 32 * h]];
+        __syncwarp();
+    }
     if (l == 0) {
         bi->nsrc = nsrc;
         bi->srcmask = nsrc >= 64 ? ~0ull : ((1ull << nsrc) - 1ull);
@@ -1424,7 +1431,8 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
                                                          const uint32_t *__restrict__ seen_,
                                                          const uint32_t *__restrict__ reach, uint64_t n,
                                                          const BatchInfo *__restrict__ bi,
-                                                         float *__restrict__ delta_out)
+                                                         float *__restrict__ delta_out,
+                                                         const uint32_t *__restrict__ from_view)
 {
     typedef typename MaskOf<K>::T M;
     constexpr int NS = AXBC_W * K;  // pivot slots
@@ -1516,6 +1524,9 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
             rvn = reach[next + lane];
         }
         const uint64_t v = base + lane;
+        // v numbers the graph's view; the bc vectors and delta_out are indexed
+        // by vertex id
+        const uint64_t vo = from_view && v < n ? from_view[v] : v;
         const float rf = __uint2float_rn(rv);
         // unreached by every pivot with delta 0: only a root term could apply,
         // and roots are reached
@@ -1527,7 +1538,7 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
         float b = 0.0f;
         if (work && single) {
             tgt = s_bc[slast];
-            b = tgt[v];
+            b = tgt[vo];
         }
 #pragma unroll 1
         for (int hh = 0; hh < K; hh++, buf ^= 1) {
@@ -1548,7 +1559,7 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
             const int s0 = 32 * hh;
             if (delta_out && v < n && (slast >> 5) == hh) {
                 const bool have = v == dl_root ? dl_root_done : ((svh >> (slast & 31)) & 1u) != 0u;
-                delta_out[v] = have ? rows[lane][slast & 31] : rf;
+                delta_out[vo] = have ? rows[lane][slast & 31] : rf;
             }
             if (sparse) {
                 for (uint32_t bits = svh & amh; bits; bits &= bits - 1) {
@@ -1586,9 +1597,9 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
                     if (!((amh >> j) & 1u)) continue;
                     const int s = s0 + j;
                     if (s_bc[s] != tgt) {
-                        if (tgt) tgt[v] = b;
+                        if (tgt) tgt[vo] = b;
                         tgt = s_bc[s];
-                        b = tgt[v];
+                        b = tgt[vo];
                     }
                     if ((uint32_t)v == s_root[s]) {
                         if (s_reach[s] > 0) b = __fadd_rn(b, bc_root_term(s_reach[s], s_nvt[s]));
@@ -1601,7 +1612,7 @@ __global__ void __launch_bounds__(UPD_TPB(K)) k_update_m(const float *__restrict
             }
             __syncwarp();
         }
-        if (tgt) tgt[v] = b;
+        if (tgt) tgt[vo] = b;
         sv = svn;
         rv = rvn;
     }
@@ -1612,7 +1623,8 @@ template <int K>
 __global__ void k_extract_delta(float *out, const float *__restrict__ mdelta,
                                 const uint32_t *__restrict__ seen_,
                                 const uint32_t *__restrict__ reach, uint64_t n,
-                                const BatchInfo *__restrict__ bi, int lane_lo, int lane_hi)
+                                const BatchInfo *__restrict__ bi, int lane_lo, int lane_hi,
+                                const uint32_t *__restrict__ from_view)
 {
     typedef typename MaskOf<K>::T M;
     const M *seen = reinterpret_cast<const M *>(seen_);
@@ -1628,7 +1640,7 @@ __global__ void k_extract_delta(float *out, const float *__restrict__ mdelta,
          v += (uint64_t)gridDim.x * blockDim.x) {
         bool have = ((unsigned long long)seen[v] >> s) & 1ull;
         if (v == root) have = root_done;
-        out[v] = have ? mdelta[row_base<K>(v) + s] : __uint2float_rn(reach[v]);
+        out[from_view ? from_view[v] : v] = have ? mdelta[row_base<K>(v) + s] : __uint2float_rn(reach[v]);
     }
 }
 
@@ -1637,7 +1649,7 @@ template <int K>
 __global__ void k_source_view(int s, int levels, uint32_t *const *fm, const uint32_t *__restrict__ seen_,
                               const uint32_t *__restrict__ msigma, const float *__restrict__ mdelta,
                               const uint32_t *__restrict__ reach, uint64_t n, unsigned long long depth0,
-                              uint32_t *sig, int32_t *lvl, float *dl)
+                              uint32_t *sig, int32_t *lvl, float *dl, const uint32_t *__restrict__ from_view)
 {
     typedef typename MaskOf<K>::T M;
     const M *seen = reinterpret_cast<const M *>(seen_);
@@ -1651,10 +1663,12 @@ __global__ void k_source_view(int s, int levels, uint32_t *const *fm, const uint
                     break;
                 }
         }
-        lvl[v] = L;
-        sig[v] = L >= 0 ? msigma[row_base<K>(v) + s] : 0u;
+        // v numbers the graph's view; the outputs are indexed by vertex id
+        const uint64_t vo = from_view ? from_view[v] : v;
+        lvl[vo] = L;
+        sig[vo] = L >= 0 ? msigma[row_base<K>(v) + s] : 0u;
         bool have = L > 0 || (L == 0 && ((depth0 >> s) & 1ull));
-        dl[v] = have ? mdelta[row_base<K>(v) + s] : __uint2float_rn(reach[v]);
+        dl[vo] = have ? mdelta[row_base<K>(v) + s] : __uint2float_rn(reach[v]);
     }
 }
 
@@ -1734,7 +1748,7 @@ int axbc_ensure_batch(axbc_ctx *c)
     ALLOC_MISSING(c->mdelta, n * AXBC_WMAX * 4, &c->bytes);
     ALLOC_MISSING(c->mq, n * AXBC_WMAX * 4, &c->bytes);
     ALLOC_MISSING(c->task_ctr, 64, &c->bytes);
-    ALLOC_MISSING(c->mpartial, (c->g->fwd.n_heavy_items + 1) * AXBC_WMAX * 4, &c->bytes);
+    ALLOC_MISSING(c->mpartial, (c->g->bfwd.n_heavy_items + 1) * AXBC_WMAX * 4, &c->bytes);
     ALLOC_MISSING(c->bi, sizeof(BatchInfo), &c->bytes);
     if (!c->bi_host) CU(cudaMallocHost((void **)&c->bi_host, sizeof(BatchInfo)));
     CU(cudaMemset(c->bi, 0, sizeof(BatchInfo)));
@@ -1771,12 +1785,12 @@ template <int K> static void fwd_step_kernels(axbc_ctx *c, int sgrid)
 {
     axbc_graph *g = c->g;
     const LevelLists ll = lists_of(c);
-    k_fwd_push_step<K, false><<<push_grid<K>(c), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->seen,
+    k_fwd_push_step<K, false><<<push_grid<K>(c), BATCH_TPB, 0, c->stream>>>(g->bfwd, c->bi, c->fmtab, c->seen,
                                                                            c->msigma, c->ctrs, ll, nullptr);
-    k_fwd_pull_step<K, false><<<pull_grid<K>(c), BATCH_TPB, 0, c->stream>>>(g->rev, c->bi, c->fmtab, c->seen,
+    k_fwd_pull_step<K, false><<<pull_grid<K>(c), BATCH_TPB, 0, c->stream>>>(g->brev, c->bi, c->fmtab, c->seen,
                                                                            c->msigma, c->ctrs, ll, nullptr);
-    k_stats_step<K><<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->fwd.col, g->rev.col,
-                                                        g->reach, ll);
+    k_stats_step<K><<<sgrid, BATCH_TPB, 0, c->stream>>>(g->n, c->bi, c->fmtab, c->seen, g->bfwd.col, g->brev.col,
+                                                        g->breach, ll);
     k_level_advance<K><<<1, 32, 0, c->stream>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode, ll,
                                                 c->lpool_cap, list_max_of(c));
 }
@@ -1784,12 +1798,12 @@ template <int K> static void fwd_step_kernels(axbc_ctx *c, int sgrid)
 template <int K> static void bwd_step_kernels(axbc_ctx *c)
 {
     axbc_graph *g = c->g;
-    k_bwd_step<K, false><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, c->stream>>>(g->fwd, c->bi, c->fmtab, c->msigma,
-                                                                     c->mdelta, c->mq, c->mpartial, g->reach,
+    k_bwd_step<K, false><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, c->stream>>>(g->bfwd, c->bi, c->fmtab, c->msigma,
+                                                                     c->mdelta, c->mq, c->mpartial, g->breach,
                                                                      c->ctrs, lists_of(c), nullptr);
-    if (g->fwd.n_heavy)
-        k_bwd_combine_step<K><<<dim3((g->fwd.n_heavy + 7) / 8, K), 256, 0, c->stream>>>(
-            g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, lists_of(c));
+    if (g->bfwd.n_heavy)
+        k_bwd_combine_step<K><<<dim3((g->bfwd.n_heavy + 7) / 8, K), 256, 0, c->stream>>>(
+            g->bfwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->breach, lists_of(c));
     k_bwd_advance<<<1, 1, 0, c->stream>>>(c->bi);
 }
 
@@ -1855,26 +1869,26 @@ template <int K> static int traverse_stepwise(axbc_ctx *c, int nsrc, int sgrid, 
                     if (c->prof_on) c->prof.back().tag = L;
                     if (wc)
                         k_fwd_push_step<K, true><<<push_grid<K>(c), BATCH_TPB, 0, s>>>(
-                            g->fwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PUSH * WC_NFIELDS);
+                            g->bfwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PUSH * WC_NFIELDS);
                     else
                         k_fwd_push_step<K, false><<<push_grid<K>(c), BATCH_TPB, 0, s>>>(
-                            g->fwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
+                            g->bfwd, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
                 }
                 {
                     ProfScope ps(c, KP_FWD_PULL, 0);
                     if (c->prof_on) c->prof.back().tag = L;
                     if (wc)
                         k_fwd_pull_step<K, true><<<pull_grid<K>(c), BATCH_TPB, 0, s>>>(
-                            g->rev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PULL * WC_NFIELDS);
+                            g->brev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, wc + KP_FWD_PULL * WC_NFIELDS);
                     else
                         k_fwd_pull_step<K, false><<<pull_grid<K>(c), BATCH_TPB, 0, s>>>(
-                            g->rev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
+                            g->brev, c->bi, c->fmtab, c->seen, c->msigma, c->ctrs, ll, nullptr);
                 }
                 {
                     ProfScope ps(c, KP_LEVEL_STATS, 0);
                     if (c->prof_on) c->prof.back().tag = L;
-                    k_stats_step<K><<<sgrid, BATCH_TPB, 0, s>>>(n, c->bi, c->fmtab, c->seen, g->fwd.col,
-                                                                g->rev.col, g->reach, ll);
+                    k_stats_step<K><<<sgrid, BATCH_TPB, 0, s>>>(n, c->bi, c->fmtab, c->seen, g->bfwd.col,
+                                                                g->brev.col, g->breach, ll);
                 }
                 k_level_advance<K><<<1, 32, 0, s>>>(c->bi, c->d_level_te, c->d_level_cnt, c->d_level_mode, ll,
                                                     c->lpool_cap, lmax);
@@ -1931,7 +1945,7 @@ template <int K> static int traverse_stepwise(axbc_ctx *c, int nsrc, int sgrid, 
         for (int d = Dmax; d >= 0; d--) {
             if (!prof) {
                 CU(cudaGraphLaunch(c->bwd_step_exec[K - 1], s));
-                c->launches += g->fwd.n_heavy ? 3 : 2;
+                c->launches += g->bfwd.n_heavy ? 3 : 2;
                 continue;
             }
             if (d == Dmax && c->prof_on) depth0 = c->bi_host->depth0mask;
@@ -1951,17 +1965,17 @@ template <int K> static int traverse_stepwise(axbc_ctx *c, int nsrc, int sgrid, 
                 if (c->prof_on) c->prof.back().tag = d;
                 if (wc)
                     k_bwd_step<K, true><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, s>>>(
-                        g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, c->ctrs, ll,
+                        g->bfwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->breach, c->ctrs, ll,
                         wc + KP_BWD * WC_NFIELDS);
                 else
                     k_bwd_step<K, false><<<dim3(bwd_grid<K>(c), K), BATCH_TPB, 0, s>>>(
-                        g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, c->ctrs, ll,
+                        g->bfwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->breach, c->ctrs, ll,
                         nullptr);
             }
-            if (g->fwd.n_heavy) {
+            if (g->bfwd.n_heavy) {
                 ProfScope ps(c, KP_BWD_COMBINE, 0);
-                k_bwd_combine_step<K><<<dim3((g->fwd.n_heavy + 7) / 8, K), 256, 0, s>>>(
-                    g->fwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->reach, ll);
+                k_bwd_combine_step<K><<<dim3((g->bfwd.n_heavy + 7) / 8, K), 256, 0, s>>>(
+                    g->bfwd, c->bi, c->fmtab, c->msigma, c->mdelta, c->mq, c->mpartial, g->breach, ll);
             }
             k_bwd_advance<<<1, 1, 0, s>>>(c->bi);
             c->launches++;
@@ -2018,9 +2032,9 @@ template <int K> static int traverse_persistent(axbc_ctx *c, int *L_out)
         c->prev_lend = levels - 1;  // masks the loop may write, cleared before the next batch
         CU(cudaMemsetAsync(c->gsync, 0, sizeof(GridSync), s));
         int lmax = levels;
-        void *args[] = {(void *)&g->fwd, (void *)&g->rev, (void *)&c->bi, (void *)&c->fmtab,
+        void *args[] = {(void *)&g->bfwd, (void *)&g->brev, (void *)&c->bi, (void *)&c->fmtab,
                         (void *)&c->seen, (void *)&c->msigma, (void *)&c->mdelta, (void *)&c->mq,
-                        (void *)&c->mpartial, (void *)&g->reach, (void *)&c->ctrs, (void *)&ll,
+                        (void *)&c->mpartial, (void *)&g->breach, (void *)&c->ctrs, (void *)&ll,
                         (void *)&c->d_level_te, (void *)&c->d_level_cnt, (void *)&c->d_level_mode,
                         (void *)&pool_cap, (void *)&lmax_list, (void *)&n, (void *)&lmax,
                         (void *)&c->gsync, (void *)&budget};
@@ -2109,11 +2123,11 @@ template <int K> static int batch_traverse(axbc_ctx *c, int nsrc, int H)
     const uint32_t lmax = list_max_of(c);
     {
         ProfScope ps(c, KP_LEVEL_STATS, 0);
-        k_batch_init<K><<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->fwd.col,
-                                         g->rev.col, g->m, c->push_factor_batch,
+        k_batch_init<K><<<1, 32, 0, s>>>(c->bi, nsrc, H, c->bc, c->fmask[0], c->seen, c->msigma, g->bfwd.col,
+                                         g->brev.col, g->m, c->push_factor_batch,
                                          // a factor of 1e30 or more pulls every level
                                          c->push_factor_batch >= 1e30 ? 0ull : (unsigned long long)(n / 4),
-                                         c->d_level_te, c->d_level_cnt, ll, c->lpool_cap, lmax);
+                                         c->d_level_te, c->d_level_cnt, ll, c->lpool_cap, lmax, g->to_view);
     }
     CU_LAUNCH("k_batch_init");
 
@@ -2173,14 +2187,15 @@ static int apply_lanes(axbc_ctx *c, float *const *delta_out, const int *lane_lo,
     {
         ProfScope ps(c, KP_UPDATE, (double)g->n * c->last_batch_nsrc * 20.0);
         // one segment over all lanes: the update writes the last delta itself
-        k_update_m<K><<<grid, UPD_TPB(K), 0, s>>>(c->mdelta, c->seen, g->reach, g->n, c->bi,
-                                                  one_seg ? (delta_out ? delta_out[0] : c->delta_last) : nullptr);
+        k_update_m<K><<<grid, UPD_TPB(K), 0, s>>>(c->mdelta, c->seen, g->breach, g->n, c->bi,
+                                                  one_seg ? (delta_out ? delta_out[0] : c->delta_last) : nullptr,
+                                                  g->from_view);
     }
     for (int i = 0; i < nseg && !one_seg; i++) {
         ProfScope ps(c, KP_UPDATE, 0);
         k_extract_delta<K><<<grid, 256, 0, s>>>(delta_out ? delta_out[i] : c->delta_last, c->mdelta, c->seen,
-                                                g->reach, g->n, c->bi, lane_lo ? lane_lo[i] : 0,
-                                                lane_hi ? lane_hi[i] : AXBC_WMAX);
+                                                g->breach, g->n, c->bi, lane_lo ? lane_lo[i] : 0,
+                                                lane_hi ? lane_hi[i] : AXBC_WMAX, g->from_view);
     }
     CU_LAUNCH("update");
     c->delta_last_valid = true;
@@ -2289,10 +2304,12 @@ extern "C" int axbc_get_batch_source(axbc_ctx *c, int src, uint32_t *sigma_host,
     CU(cudaStreamSynchronize(s));
     if (c->last_batch_k == 2)
         k_source_view<2><<<axbc_grid_for(c, 256, 4), 256, 0, s>>>(src, levels, d_fm, c->seen, c->msigma, c->mdelta,
-                                                                  c->g->reach, n, depth0, sig, lvl, dl);
+                                                                  c->g->breach, n, depth0, sig, lvl, dl,
+                                                                  c->g->from_view);
     else
         k_source_view<1><<<axbc_grid_for(c, 256, 4), 256, 0, s>>>(src, levels, d_fm, c->seen, c->msigma, c->mdelta,
-                                                                  c->g->reach, n, depth0, sig, lvl, dl);
+                                                                  c->g->breach, n, depth0, sig, lvl, dl,
+                                                                  c->g->from_view);
     CU_LAUNCH("k_source_view");
     if (sigma_host) CU(cudaMemcpyAsync(sigma_host, sig, n * 4, cudaMemcpyDeviceToHost, s));
     if (lvl_host) CU(cudaMemcpyAsync(lvl_host, lvl, n * 4, cudaMemcpyDeviceToHost, s));

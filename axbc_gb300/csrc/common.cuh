@@ -85,6 +85,17 @@ struct axbc_graph {
     int symmetric = 1;
     Adj fwd, rev;
     uint32_t *reach = nullptr;  // n
+    // The batched passes' view of the graph.  On graphs with a vertex of more
+    // than AXBC_RENUMBER_MIN_DEG neighbours the vertices are renumbered by
+    // descending degree (ties by id), so that the hubs' level-mask words and
+    // per-pivot rows share sectors and lines; every adjacency list keeps its
+    // own order (the canonical dependency sums run over the same positions).
+    // Otherwise the view is the graph itself (aliases, null maps).
+    bool renumbered = false;
+    Adj bfwd, brev;
+    uint32_t *breach = nullptr;     // reach in view numbering
+    uint32_t *to_view = nullptr;    // n: view id of each vertex (null: identity)
+    uint32_t *from_view = nullptr;  // n: vertex of each view id (null: identity)
     uint64_t bytes = 0;
     uint32_t max_deg = 0;
     // static pivot distributions, built on first use
@@ -176,6 +187,11 @@ struct GridSync {
 // batches of at most AXBC_PERSIST_AUTO_WIDTH pivots on graphs whose last batch
 // was deeper than AXBC_PERSIST_AUTO_LEVELS run their levels in one persistent
 // launch
+// graphs whose largest degree exceeds this are renumbered for the batched
+// passes (meshes and road-like graphs keep their own, already local, order)
+#ifndef AXBC_RENUMBER_MIN_DEG
+#define AXBC_RENUMBER_MIN_DEG 64
+#endif
 #ifndef AXBC_PERSIST_AUTO_LEVELS
 #define AXBC_PERSIST_AUTO_LEVELS 64
 #endif

@@ -137,15 +137,10 @@ static void task_tables(const uint32_t *col, uint64_t n, std::vector<uint32_t> &
     ltask.push_back((uint32_t)n);
 }
 
-static int upload_adj(Adj &a, const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
-                      uint64_t *acct, uint32_t *maxdeg)
+// heavy-vertex span items and light-vertex tasks of an adjacency whose col
+// (host copy: col) is on the device
+static int adj_tables(Adj &a, const uint32_t *col, uint64_t n, uint64_t *acct, uint32_t *maxdeg)
 {
-    a.n = n;
-    a.m = m;
-    TRY(axbc_dalloc((void **)&a.col, (n + 1) * 4, acct));
-    TRY(axbc_dalloc((void **)&a.row, m * 4, acct));
-    CU(cudaMemcpy(a.col, col, (n + 1) * 4, cudaMemcpyHostToDevice));
-    if (m) CU(cudaMemcpy(a.row, row, m * 4, cudaMemcpyHostToDevice));
     std::vector<uint32_t> hv, hf, iv, ik;
     heavy_lists(col, n, hv, hf, iv, ik, maxdeg);
     a.n_heavy = (uint32_t)hv.size();
@@ -168,7 +163,112 @@ static int upload_adj(Adj &a, const uint32_t *col, const uint32_t *row, uint64_t
     TRY(axbc_dalloc((void **)&a.ltask, ltask.size() * 4, acct));
     CU(cudaMemcpy(a.order, order.data(), n * 4, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(a.ltask, ltask.data(), ltask.size() * 4, cudaMemcpyHostToDevice));
+    return AXBC_OK;
+}
+
+static int upload_adj(Adj &a, const uint32_t *col, const uint32_t *row, uint64_t n, uint64_t m,
+                      uint64_t *acct, uint32_t *maxdeg)
+{
+    a.n = n;
+    a.m = m;
     a.owns = true;
+    TRY(axbc_dalloc((void **)&a.col, (n + 1) * 4, acct));
+    TRY(axbc_dalloc((void **)&a.row, m * 4, acct));
+    CU(cudaMemcpy(a.col, col, (n + 1) * 4, cudaMemcpyHostToDevice));
+    if (m) CU(cudaMemcpy(a.row, row, m * 4, cudaMemcpyHostToDevice));
+    return adj_tables(a, col, n, acct, maxdeg);
+}
+
+// ------------------------------------------------------------ batch view
+
+// view adjacency: the list of view vertex i is the list of vertex order[i],
+// in its own order, its entries renumbered (one warp per vertex)
+__global__ void k_view_rows(const uint32_t *__restrict__ col, const uint32_t *__restrict__ row,
+                            const uint32_t *__restrict__ order, const uint32_t *__restrict__ to_view,
+                            const uint32_t *__restrict__ vcol, uint32_t *__restrict__ vrow, uint64_t n)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; i < n; i += nw) {
+        const uint32_t v = order[i];
+        const uint32_t b = col[v], d = col[v + 1] - b, o = vcol[i];
+        for (uint32_t k = lane; k < d; k += 32) vrow[o + k] = to_view[row[b + k]];
+    }
+}
+
+__global__ void k_view_gather(const uint32_t *__restrict__ src, const uint32_t *__restrict__ order,
+                              uint32_t *__restrict__ dst, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[order[i]];
+}
+
+// src (on the device, host copy of its col: col) in view numbering
+static int view_adj(Adj &dst, const Adj &src, const uint32_t *col, const std::vector<uint32_t> &order,
+                    const uint32_t *d_order, const uint32_t *d_to_view, uint64_t *acct)
+{
+    const uint64_t n = src.n, m = src.m;
+    std::vector<uint32_t> vcol(n + 1);
+    vcol[0] = 0;
+    for (uint64_t i = 0; i < n; i++) vcol[i + 1] = vcol[i] + (col[order[i] + 1] - col[order[i]]);
+    dst.n = n;
+    dst.m = m;
+    dst.owns = true;
+    TRY(axbc_dalloc((void **)&dst.col, (n + 1) * 4, acct));
+    TRY(axbc_dalloc((void **)&dst.row, m * 4, acct));
+    CU(cudaMemcpy(dst.col, vcol.data(), (n + 1) * 4, cudaMemcpyHostToDevice));
+    if (m) {
+        k_view_rows<<<2048, 256>>>(src.col, src.row, d_order, d_to_view, dst.col, dst.row, n);
+        CU_LAUNCH("k_view_rows");
+    }
+    return adj_tables(dst, vcol.data(), n, acct, nullptr);
+}
+
+// The batched passes' view (see axbc_graph): renumbered by descending degree
+// when the largest degree exceeds AXBC_RENUMBER_MIN_DEG, else the graph itself.
+static int build_view(axbc_graph *g, const uint32_t *col, const uint32_t *tcol)
+{
+    const uint64_t n = g->n;
+    if (g->max_deg <= AXBC_RENUMBER_MIN_DEG || n < 2) {
+        g->bfwd = g->fwd;
+        g->bfwd.owns = false;
+        g->brev = g->rev;
+        g->brev.owns = false;
+        g->breach = g->reach;
+        g->renumbered = false;
+        return AXBC_OK;
+    }
+    g->renumbered = true;
+    // descending degree, ties by id (counting sort)
+    uint32_t md = 0;
+    for (uint64_t v = 0; v < n; v++) md = std::max(md, col[v + 1] - col[v]);
+    std::vector<uint64_t> cnt((size_t)md + 2, 0);
+    for (uint64_t v = 0; v < n; v++) cnt[md - (col[v + 1] - col[v])]++;
+    uint64_t acc = 0;
+    for (auto &c : cnt) {
+        const uint64_t t = c;
+        c = acc;
+        acc += t;
+    }
+    std::vector<uint32_t> order(n), to_view(n);
+    for (uint64_t v = 0; v < n; v++) order[cnt[md - (col[v + 1] - col[v])]++] = (uint32_t)v;
+    for (uint64_t i = 0; i < n; i++) to_view[order[i]] = (uint32_t)i;
+    TRY(axbc_dalloc((void **)&g->from_view, n * 4, &g->bytes));
+    TRY(axbc_dalloc((void **)&g->to_view, n * 4, &g->bytes));
+    TRY(axbc_dalloc((void **)&g->breach, n * 4, &g->bytes));
+    CU(cudaMemcpy(g->from_view, order.data(), n * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(g->to_view, to_view.data(), n * 4, cudaMemcpyHostToDevice));
+    k_view_gather<<<1024, 256>>>(g->reach, g->from_view, g->breach, n);
+    CU_LAUNCH("k_view_gather");
+    TRY(view_adj(g->bfwd, g->fwd, col, order, g->from_view, g->to_view, &g->bytes));
+    if (g->symmetric) {
+        g->brev = g->bfwd;
+        g->brev.owns = false;
+    } else {
+        TRY(view_adj(g->brev, g->rev, tcol, order, g->from_view, g->to_view, &g->bytes));
+    }
+    CU(cudaDeviceSynchronize());
     return AXBC_OK;
 }
 
@@ -240,6 +340,11 @@ static int graph_from_host(const uint32_t *col, const uint32_t *row, uint64_t n,
     }
     if (reach) CU(cudaMemcpy(g->reach, reach, n * 4, cudaMemcpyHostToDevice));
     else CU(cudaMemset(g->reach, 0, n * 4));
+    rc = build_view(g, col, sym ? col : tcol.data());
+    if (rc) {
+        axbc_graph_destroy(g);
+        return rc;
+    }
     *out = g;
     return AXBC_OK;
 }
@@ -260,6 +365,13 @@ extern "C" int axbc_graph_create(const uint32_t *col, const uint32_t *row, uint6
 extern "C" int axbc_graph_destroy(axbc_graph *g)
 {
     if (!g) return AXBC_OK;
+    free_adj(g->brev);
+    free_adj(g->bfwd);
+    if (g->renumbered) {
+        axbc_dfree(g->breach);
+        axbc_dfree(g->to_view);
+        axbc_dfree(g->from_view);
+    }
     free_adj(g->rev);
     free_adj(g->fwd);
     axbc_dfree(g->reach);

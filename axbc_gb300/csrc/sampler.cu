@@ -568,7 +568,7 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
                                const float *__restrict__ mdelta, const uint32_t *__restrict__ seen,
                                const uint32_t *__restrict__ reach, const uint32_t *__restrict__ checks,
                                float *b, uint32_t *hist_v, double *hist_p, uint64_t hist_cap,
-                               int off, int lane0, int cnt, int K)
+                               int off, int lane0, int cnt, int K, const uint32_t *__restrict__ to_view)
 {
     if (ss->done && ss->nb == 0) return;
     const int nb = max(0, min(min(ss->nb - off, AXBC_WMAX - lane0), cnt));
@@ -602,8 +602,9 @@ __global__ void k_sampler_post(SamplerState *ss, BatchInfo *bi, const float *__r
         const unsigned long long nvt = bi->nvis[l] + all;
         const double p = bi->p[l];
         for (uint32_t i = 0; i < x; i++) {
-            const uint32_t v = checks[i];
-            if (v >= N) continue;
+            if (checks[i] >= N) continue;
+            // the pass runs in the graph's view (roots, masks, rows, reach)
+            const uint32_t v = to_view ? to_view[checks[i]] : checks[i];
             if (v == r) {
                 if (rr > 0) b[i] = __fadd_rn(b[i], bc_root_term(rr, nvt));
                 continue;
@@ -874,9 +875,10 @@ int sr_post(axbc_ctx *c, SampledRun *r, int off, int lane0, int cnt)
 {
     {
         ProfScope ps(c, KP_SAMPLER, 0);
-        k_sampler_post<<<1, 1, 0, c->stream>>>(r->ss, c->bi, r->bc, c->mdelta, c->seen, c->g->reach,
+        k_sampler_post<<<1, 1, 0, c->stream>>>(r->ss, c->bi, r->bc, c->mdelta, c->seen, c->g->breach,
                                                r->checks, r->checkval, r->hist_v, r->hist_p,
-                                               r->hist_cap, off, lane0, cnt, c->last_batch_k);
+                                               r->hist_cap, off, lane0, cnt, c->last_batch_k,
+                                               c->g->to_view);
     }
     CU_LAUNCH("k_sampler_post");
     return AXBC_OK;
